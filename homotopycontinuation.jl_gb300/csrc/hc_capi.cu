@@ -1,0 +1,702 @@
+// hc_capi.cu — the extern "C" boundary of libhcgpu.so (declared in include/hcgpu.h):
+// handle and option management, the host-side compilation of a homotopy into a monomial
+// program with a static lane schedule, and the batched track calls.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "hc_dev.h"
+
+namespace hcd {
+cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaStream_t stream);
+cudaError_t occupancy(int precision, int warps_per_cta, size_t smem, int* blocks_per_sm);
+}  // namespace hcd
+
+using namespace hcd;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_err;
+
+struct Term {
+  int row;
+  int mono;
+  double re, im;
+  int vterm;  // Jacobian terms: index of the value term supplying the coefficient
+  int mult;   // Jacobian terms: exponent multiplier
+  int orig;   // value terms: position in the caller's order
+};
+
+// Host copy of a compiled homotopy
+struct HostProg {
+  int n = 0, M = 0, nlev = 0, top = 0;
+  std::vector<int2> mdef;
+  std::vector<int> lev;
+  struct Rows {
+    int nrows = 0, nslots = 0;
+    std::vector<int4> seg;
+    std::vector<int> lane_seg, row_slot;
+  } val, jac;
+  std::vector<double2> vcoef64;
+  std::vector<float2> vcoef32;
+  std::vector<uint16_t> vmono;
+  std::vector<uint32_t> jcode;
+  // operation census for the flop model
+  long long val_terms = 0, jac_terms = 0;
+};
+
+// Monomial table closed under "parent" (drop one power of the first variable) and under
+// the derivative monomials the Jacobian rows need; degree-ordered levels.
+struct MonoTable {
+  int n;
+  std::map<std::vector<int>, int> idx;
+  std::vector<std::vector<int>> list;
+  explicit MonoTable(int nn) : n(nn) {}
+  void insert(const std::vector<int>& e) {
+    if (idx.count(e)) return;
+    int deg = 0, v = -1;
+    for (int j = 0; j < n; ++j) {
+      deg += e[j];
+      if (v < 0 && e[j] > 0) v = j;
+    }
+    if (deg > 0) {
+      std::vector<int> p = e;
+      p[v] -= 1;
+      insert(p);
+    }
+    idx[e] = -1;
+    list.push_back(e);
+  }
+};
+
+// Cut rows (terms sorted by row, then by multiplier) into segments of one multiplier and at
+// most ~T/(32*per_lane) terms, and spread them over the 32 lanes (longest first to the least
+// loaded lane). Slots are numbered row-major so a row's partials are contiguous.
+void build_segments(int nrows, const std::vector<Term>& terms, int per_lane, HostProg::Rows& R) {
+  R.nrows = nrows;
+  int T = (int)terms.size();
+  std::vector<int> row_begin(nrows + 1, 0);
+  for (int k = 0; k < T; ++k) row_begin[terms[k].row + 1] += 1;
+  for (int r = 0; r < nrows; ++r) row_begin[r + 1] += row_begin[r];
+  int L = std::max(8, (T + 32 * per_lane - 1) / (32 * per_lane));
+  struct Chunk {
+    int row, b, e, slot, mult;
+  };
+  std::vector<Chunk> chunks;
+  R.row_slot.assign(nrows + 1, 0);
+  for (int r = 0; r < nrows; ++r) {
+    int b = row_begin[r], e = row_begin[r + 1];
+    int k = b;
+    while (k < e) {  // runs of equal multiplier
+      int k2 = k;
+      while (k2 < e && terms[k2].mult == terms[k].mult) ++k2;
+      int t = k2 - k;
+      int nc = (t + L - 1) / L;
+      for (int c = 0; c < nc; ++c) {
+        int cb = k + (int)((long long)t * c / nc), ce = k + (int)((long long)t * (c + 1) / nc);
+        chunks.push_back({r, cb, ce, (int)chunks.size(), terms[k].mult});
+      }
+      k = k2;
+    }
+    R.row_slot[r + 1] = (int)chunks.size();
+  }
+  R.nslots = (int)chunks.size();
+  std::vector<int> order(chunks.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (chunks[a].e - chunks[a].b) > (chunks[b].e - chunks[b].b);
+  });
+  std::vector<long long> load(32, 0);
+  std::vector<std::vector<int>> lane_chunks(32);
+  for (int ci : order) {
+    int best = 0;
+    for (int l = 1; l < 32; ++l)
+      if (load[l] < load[best]) best = l;
+    load[best] += chunks[ci].e - chunks[ci].b + 2;
+    lane_chunks[best].push_back(ci);
+  }
+  R.seg.clear();
+  R.lane_seg.assign(33, 0);
+  for (int l = 0; l < 32; ++l) {
+    std::sort(lane_chunks[l].begin(), lane_chunks[l].end());
+    for (int ci : lane_chunks[l])
+      R.seg.push_back(make_int4(chunks[ci].row, chunks[ci].b, chunks[ci].e,
+                                chunks[ci].slot | (chunks[ci].mult << 24)));
+    R.lane_seg[l + 1] = (int)R.seg.size();
+  }
+}
+
+int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const double* G_coef, int nF,
+                  const int32_t* F_eq, const int32_t* F_exps, const double* F_coef, HostProg& P,
+                  std::string& err) {
+  MonoTable mt(n);
+  std::vector<int> zero(n, 0);
+  mt.insert(zero);
+  std::vector<int> e(n);
+  int maxexp = 0;
+  auto visit = [&](int cnt, const int32_t* eqs, const int32_t* exps) -> bool {
+    for (int k = 0; k < cnt; ++k) {
+      if (eqs[k] < 0 || eqs[k] >= n) return false;
+      for (int j = 0; j < n; ++j) {
+        e[j] = exps[(size_t)k * n + j];
+        if (e[j] < 0) return false;
+        maxexp = std::max(maxexp, e[j]);
+      }
+      mt.insert(e);
+      for (int j = 0; j < n; ++j)
+        if (e[j] > 0) {
+          std::vector<int> d = e;
+          d[j] -= 1;
+          mt.insert(d);
+        }
+    }
+    return true;
+  };
+  if (!visit(nG, G_eq, G_exps) || !visit(nF, F_eq, F_exps)) {
+    err = "term table has an equation index outside [0,n) or a negative exponent";
+    return HC_ERR_INVALID_ARG;
+  }
+  if (mt.list.size() > 65535 || (size_t)nG + nF > 65535) {
+    err = "homotopy needs more than 65535 monomials or value terms";
+    return HC_ERR_TOO_LARGE;
+  }
+  if (maxexp > 255) {
+    err = "exponents above 255 are not supported";
+    return HC_ERR_TOO_LARGE;
+  }
+  std::vector<std::vector<int>> mons = mt.list;
+  std::stable_sort(mons.begin(), mons.end(), [](const std::vector<int>& a, const std::vector<int>& b) {
+    int da = std::accumulate(a.begin(), a.end(), 0), db = std::accumulate(b.begin(), b.end(), 0);
+    if (da != db) return da < db;
+    return a > b;
+  });
+  std::map<std::vector<int>, int> index;
+  for (size_t i = 0; i < mons.size(); ++i) index[mons[i]] = (int)i;
+  P.n = n;
+  P.M = (int)mons.size();
+  P.mdef.assign(P.M, make_int2(0, 0));
+  int maxdeg = 0;
+  for (int m = 1; m < P.M; ++m) {
+    const std::vector<int>& me = mons[m];
+    int v = 0;
+    while (me[v] == 0) ++v;
+    std::vector<int> p = me;
+    p[v] -= 1;
+    P.mdef[m] = make_int2(index[p], v);
+    maxdeg = std::max(maxdeg, std::accumulate(me.begin(), me.end(), 0));
+  }
+  P.lev.assign(maxdeg + 2, 0);
+  {
+    int cur = 0;
+    for (int d = 0; d <= maxdeg; ++d) {
+      P.lev[d] = cur;
+      while (cur < P.M && std::accumulate(mons[cur].begin(), mons[cur].end(), 0) == d) ++cur;
+    }
+    P.lev[maxdeg + 1] = cur;
+  }
+  P.nlev = maxdeg + 1;
+  P.top = P.lev[maxdeg];
+  // value terms (rows F_0..F_{n-1}, G_0..G_{n-1}) in caller order, then stably sorted by row
+  std::vector<Term> vt;
+  std::vector<std::vector<int>> vexp;
+  auto addv = [&](int cnt, const int32_t* eqs, const int32_t* exps, const double* cf, int rowoff) {
+    for (int k = 0; k < cnt; ++k) {
+      for (int j = 0; j < n; ++j) e[j] = exps[(size_t)k * n + j];
+      vt.push_back({rowoff + eqs[k], index[e], cf[2 * k], cf[2 * k + 1], 0, 1, (int)vt.size()});
+      vexp.push_back(e);
+    }
+  };
+  addv(nF, F_eq, F_exps, F_coef, 0);
+  addv(nG, G_eq, G_exps, G_coef, n);
+  std::stable_sort(vt.begin(), vt.end(), [](const Term& a, const Term& b) { return a.row < b.row; });
+  P.vcoef64.resize(vt.size());
+  P.vcoef32.resize(vt.size());
+  P.vmono.resize(vt.size());
+  for (size_t k = 0; k < vt.size(); ++k) {
+    P.vcoef64[k] = make_double2(vt[k].re, vt[k].im);
+    P.vcoef32[k] = make_float2((float)vt[k].re, (float)vt[k].im);
+    P.vmono[k] = (uint16_t)vt[k].mono;
+  }
+  // Jacobian terms: ∂/∂x_j of value term k → (row, monomial e - e_j, value term k, e_j)
+  std::vector<Term> jt;
+  for (size_t k = 0; k < vt.size(); ++k) {
+    const std::vector<int>& ex = vexp[vt[k].orig];
+    int eq = vt[k].row < n ? vt[k].row : vt[k].row - n;
+    int off = vt[k].row < n ? 0 : n * n;
+    for (int j = 0; j < n; ++j)
+      if (ex[j] > 0) {
+        std::vector<int> d = ex;
+        d[j] -= 1;
+        jt.push_back({off + j * n + eq, index[d], 0, 0, (int)k, ex[j], 0});
+      }
+  }
+  std::stable_sort(jt.begin(), jt.end(), [](const Term& a, const Term& b) {
+    return a.row != b.row ? a.row < b.row : a.mult < b.mult;
+  });
+  P.jcode.resize(jt.size());
+  for (size_t k = 0; k < jt.size(); ++k) P.jcode[k] = (uint32_t)jt[k].mono | ((uint32_t)jt[k].vterm << 16);
+  P.val_terms = (long long)vt.size();
+  P.jac_terms = (long long)jt.size();
+  build_segments(2 * n, vt, 2, P.val);
+  build_segments(2 * n * n, jt, 4, P.jac);
+  return HC_OK;
+}
+
+inline int pad16(size_t b) { return (int)((b + 15) & ~(size_t)15); }
+
+TableLayout make_table_layout(const HostProg& P, int precision) {
+  TableLayout T{};
+  int off = 0;
+  T.n64 = pad16(P.vcoef64.size() * sizeof(double2));
+  T.n32 = precision == HC_PREC_MIXED ? pad16(P.vcoef32.size() * sizeof(float2)) : 0;
+  T.nmono = pad16(P.vmono.size() * sizeof(uint16_t));
+  T.njcode = pad16(P.jcode.size() * sizeof(uint32_t));
+  T.nmdef = pad16(P.mdef.size() * sizeof(int2));
+  T.vcoef64 = off;
+  off += T.n64;
+  T.vcoef32 = off;
+  off += T.n32;
+  T.vmono = off;
+  off += T.nmono;
+  T.jcode = off;
+  off += T.njcode;
+  T.mdef = off;
+  off += T.nmdef;
+  T.bytes = off;
+  return T;
+}
+
+WarpLayout make_warp_layout(const HostProg& P) {
+  WarpLayout L{};
+  int n = P.n;
+  int vn = (n + 1) & ~1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 15) & ~(size_t)15;
+    return (int)o;
+  };
+  L.state = take(HC_STATE_BYTES);
+  size_t series = (size_t)16 * (4 * (size_t)P.top + 2 * (size_t)(P.M - P.top));
+  L.mono = take(std::max({(size_t)P.M * 32, (size_t)P.M * 24, series}));
+  size_t part = std::max({(size_t)P.val.nslots * 32, (size_t)P.jac.nslots * 16, (size_t)16});
+  L.part = take(part);
+  L.A = take((size_t)n * n * 16);
+  L.LU = take((size_t)n * n * 16);
+  L.xJ = take((size_t)vn * 16);
+  L.dinv = take((size_t)vn * 16);
+  L.ipiv = take(32 * 4);
+  L.vec = take((size_t)HC_NCVEC * vn * 16);
+  L.rvec = take((size_t)HC_NRVEC * vn * 8);
+  L.vn = vn;
+  L.bytes = (int)off;
+  return L;
+}
+
+}  // namespace
+
+struct hc_handle {
+  hc_options opts;
+  cudaStream_t stream = nullptr;
+  int device = 0, num_sms = 0;
+  std::string err;
+  // program
+  HostProg prog;
+  bool has_prog = false;
+  char* d_prog = nullptr;
+  size_t d_prog_bytes = 0;
+  DevProg dprog{};
+  WarpLayout layout{};
+  // buffers
+  double2* d_starts = nullptr;
+  hc_path_result* d_res = nullptr;
+  double2* d_sol = nullptr;
+  double* d_val = nullptr;
+  double2* d_last = nullptr;
+  int64_t cap_paths = 0;
+  unsigned long long* d_counter = nullptr;  // [1 + 8 stats]
+  int* h_cancel = nullptr;                  // mapped host memory
+  int* d_cancel = nullptr;
+  double stats[8] = {0};
+  int last_blocks = 0, last_wpc = 0;
+  // step log
+  double* d_log = nullptr;
+  unsigned long long* d_log_count = nullptr;
+  long long log_cap = 0, log_lo = 0, log_hi = 0;
+};
+
+static int fail(hc_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  std::lock_guard<std::mutex> g(g_err_mu);
+  g_err = msg;
+  return code;
+}
+static int cuda_fail(hc_handle* h, cudaError_t e, const char* where) {
+  return fail(h, HC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cuda_fail(h, _e, #call); \
+  } while (0)
+
+extern "C" {
+
+int hc_default_options(hc_options* o) {
+  if (!o) return fail(nullptr, HC_ERR_INVALID_ARG, "hc_default_options: null pointer");
+  memset(o, 0, sizeof(*o));
+  o->max_steps = 10000;
+  o->extended_precision = 1;
+  o->max_step_size = INFINITY;
+  o->max_initial_step_size = INFINITY;
+  o->min_step_size = 1e-48;
+  o->min_rel_step_size = 0.0;
+  o->terminate_cond = 1e13;
+  o->a = 0.125;
+  o->beta_a = 1.0;
+  o->beta_omega_p = 3.0;
+  o->beta_tau = 0.4;
+  o->strict_beta_tau = 0.3;
+  o->min_newton_iters = 2;
+  o->max_endgame_steps = 2000;
+  o->max_endgame_extended_steps = 400;
+  o->max_winding_number = 6;
+  o->zero_is_at_infinity = 0;
+  o->at_infinity_check = 1;
+  o->only_nonsingular = 0;
+  o->refine_steps = 3;
+  o->endgame_start = 0.1;
+  o->min_cond = 1e6;
+  o->min_cond_growth = 1e4;
+  o->min_coord_growth = 100.0;
+  o->singular_min_accuracy = 1e-6;
+  o->val_finite_tol = 0.05;
+  o->val_at_infinity_tol = 0.01;
+  o->sing_cond = 1e14;
+  o->sing_accuracy = 1e-12;
+  o->scaling_threshold = -30.0;
+  o->precision = HC_PREC_FP64;
+  o->step_control = HC_STEP_PLAIN;
+  o->warps_per_cta = 0;
+  o->ctas_per_sm = 0;
+  return HC_OK;
+}
+
+int hc_create(const hc_options* opts, hc_handle** out) {
+  if (!out) return fail(nullptr, HC_ERR_INVALID_ARG, "hc_create: null output pointer");
+  *out = nullptr;
+  hc_handle* h = new hc_handle();
+  if (opts)
+    h->opts = *opts;
+  else
+    hc_default_options(&h->opts);
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, 9 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaHostAlloc(&h->h_cancel, sizeof(int), cudaHostAllocMapped);
+  if (e == cudaSuccess) {
+    *h->h_cancel = 0;
+    e = cudaHostGetDevicePointer(&h->d_cancel, h->h_cancel, 0);
+  }
+  if (e != cudaSuccess) {
+    int rc = cuda_fail(nullptr, e, "hc_create");
+    hc_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return HC_OK;
+}
+
+void hc_destroy(hc_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->d_prog);
+  cudaFree(h->d_starts);
+  cudaFree(h->d_res);
+  cudaFree(h->d_sol);
+  cudaFree(h->d_val);
+  cudaFree(h->d_last);
+  cudaFree(h->d_counter);
+  cudaFree(h->d_log);
+  cudaFree(h->d_log_count);
+  if (h->h_cancel) cudaFreeHost(h->h_cancel);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int hc_set_options(hc_handle* h, const hc_options* opts) {
+  if (!h || !opts) return fail(h, HC_ERR_INVALID_ARG, "hc_set_options: null pointer");
+  if (opts->precision != HC_PREC_FP64 && opts->precision != HC_PREC_MIXED)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_options: unknown precision");
+  h->opts = *opts;
+  return HC_OK;
+}
+
+int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
+                    const double* G_coef, int nF, const int32_t* F_eq, const int32_t* F_exps,
+                    const double* F_coef, double gamma_re, double gamma_im) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_homotopy: null handle");
+  if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_set_homotopy: need 1 <= n <= 32");
+  if (nG < 0 || nF < 0 || (nG > 0 && (!G_eq || !G_exps || !G_coef)) || (nF > 0 && (!F_eq || !F_exps || !F_coef)))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_homotopy: bad term table");
+  if (!std::isfinite(gamma_re) || !std::isfinite(gamma_im))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_homotopy: gamma must be finite");
+  HostProg P;
+  std::string err;
+  int rc = build_program(n, nG, G_eq, G_exps, G_coef, nF, F_eq, F_exps, F_coef, P, err);
+  if (rc != HC_OK) return fail(h, rc, "hc_set_homotopy: " + err);
+  WarpLayout L = make_warp_layout(P);
+  TableLayout T = make_table_layout(P, HC_PREC_MIXED);
+  if ((size_t)T.bytes + L.bytes > 220 * 1024)
+    return fail(h, HC_ERR_TOO_LARGE, "hc_set_homotopy: tables plus one path's working set exceed shared memory");
+  // pack device arrays (16-byte aligned, each padded to a multiple of 16 bytes)
+  std::vector<char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    size_t o = (blob.size() + 15) & ~(size_t)15;
+    blob.resize(o + ((bytes + 15) & ~(size_t)15), 0);
+    if (bytes) memcpy(blob.data() + o, src, bytes);
+    return o;
+  };
+  size_t o_mdef = put(P.mdef.data(), P.mdef.size() * sizeof(int2));
+  size_t o_lev = put(P.lev.data(), P.lev.size() * sizeof(int));
+  size_t o_c64 = put(P.vcoef64.data(), P.vcoef64.size() * sizeof(double2));
+  size_t o_c32 = put(P.vcoef32.data(), P.vcoef32.size() * sizeof(float2));
+  size_t o_mono = put(P.vmono.data(), P.vmono.size() * sizeof(uint16_t));
+  size_t o_jcode = put(P.jcode.data(), P.jcode.size() * sizeof(uint32_t));
+  size_t off[2][3];
+  HostProg::Rows* rows[2] = {&P.val, &P.jac};
+  for (int q = 0; q < 2; ++q) {
+    HostProg::Rows& R = *rows[q];
+    off[q][0] = put(R.seg.data(), R.seg.size() * sizeof(int4));
+    off[q][1] = put(R.lane_seg.data(), R.lane_seg.size() * sizeof(int));
+    off[q][2] = put(R.row_slot.data(), R.row_slot.size() * sizeof(int));
+  }
+  if (h->d_prog_bytes < blob.size()) {
+    cudaFree(h->d_prog);
+    h->d_prog = nullptr;
+    h->d_prog_bytes = 0;
+    CK(cudaMalloc(&h->d_prog, blob.size()));
+    h->d_prog_bytes = blob.size();
+  }
+  CK(cudaMemcpyAsync(h->d_prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  DevProg D{};
+  D.n = n;
+  D.M = P.M;
+  D.nlev = P.nlev;
+  D.top = P.top;
+  D.mdef = (const int2*)(h->d_prog + o_mdef);
+  D.lev = (const int*)(h->d_prog + o_lev);
+  D.vcoef64 = (const double2*)(h->d_prog + o_c64);
+  D.vcoef32 = (const float2*)(h->d_prog + o_c32);
+  D.vmono = (const uint16_t*)(h->d_prog + o_mono);
+  D.jcode = (const uint32_t*)(h->d_prog + o_jcode);
+  DevRows* drows[2] = {&D.val, &D.jac};
+  for (int q = 0; q < 2; ++q) {
+    HostProg::Rows& R = *rows[q];
+    DevRows& X = *drows[q];
+    X.nrows = R.nrows;
+    X.nterms = q == 0 ? (int)P.vcoef64.size() : (int)P.jcode.size();
+    X.nslots = R.nslots;
+    X.nseg = (int)R.seg.size();
+    X.seg = (const int4*)(h->d_prog + off[q][0]);
+    X.lane_seg = (const int*)(h->d_prog + off[q][1]);
+    X.row_slot = (const int*)(h->d_prog + off[q][2]);
+  }
+  D.gamma_re = gamma_re;
+  D.gamma_im = gamma_im;
+  h->prog = std::move(P);
+  h->dprog = D;
+  h->layout = L;
+  h->has_prog = true;
+  return HC_OK;
+}
+
+static int ensure_capacity(hc_handle* h, int64_t npaths, int n) {
+  if (npaths <= h->cap_paths) return HC_OK;
+  cudaFree(h->d_starts);
+  cudaFree(h->d_res);
+  cudaFree(h->d_sol);
+  cudaFree(h->d_val);
+  cudaFree(h->d_last);
+  h->d_starts = nullptr;
+  h->d_res = nullptr;
+  h->d_sol = nullptr;
+  h->d_val = nullptr;
+  h->d_last = nullptr;
+  h->cap_paths = 0;
+  size_t nv = (size_t)npaths * n;
+  CK(cudaMalloc(&h->d_starts, nv * sizeof(double2)));
+  CK(cudaMalloc(&h->d_res, (size_t)npaths * sizeof(hc_path_result)));
+  CK(cudaMalloc(&h->d_sol, nv * sizeof(double2)));
+  CK(cudaMalloc(&h->d_val, nv * sizeof(double)));
+  CK(cudaMalloc(&h->d_last, nv * sizeof(double2)));
+  h->cap_paths = npaths;
+  return HC_OK;
+}
+
+int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
+                    double t1_im, double t0_re, double t0_im, hc_path_result* d_results, double* d_solutions,
+                    double* d_valuation, double* d_last, void* stream) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null handle");
+  if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_device: call hc_set_homotopy first");
+  if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: npaths < 0");
+  if (npaths == 0) return HC_OK;
+  if (!d_starts || !d_results || !d_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  Launch la{};
+  la.P = h->dprog;
+  la.O = h->opts;
+  la.L = h->layout;
+  la.T = make_table_layout(h->prog, h->opts.precision);
+  la.npaths = npaths;
+  la.starts = (const double2*)d_starts;
+  la.res = d_results;
+  la.sol = (double2*)d_solutions;
+  la.val = d_valuation;
+  la.last = (double2*)d_last;
+  la.mode = endgame ? 1 : 0;
+  la.t1_re = t1_re;
+  la.t1_im = t1_im;
+  la.t0_re = t0_re;
+  la.t0_im = t0_im;
+  la.counter = h->d_counter;
+  la.cancel = h->d_cancel;
+  la.stats = h->d_counter + 1;
+  la.log = h->log_cap > 0 ? h->d_log : nullptr;
+  la.log_count = h->d_log_count;
+  la.log_cap = h->log_cap;
+  la.log_lo = h->log_lo;
+  la.log_hi = h->log_hi;
+  if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
+  // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
+  const size_t smem_cap = 227 * 1024;
+  int wpc = h->opts.warps_per_cta;
+  if (wpc <= 0) {
+    wpc = (int)std::min<size_t>(8, (smem_cap - la.T.bytes) / la.L.bytes);
+    wpc = std::max(wpc, 1);
+  }
+  size_t smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
+  while (wpc > 1 && smem > smem_cap) {
+    --wpc;
+    smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
+  }
+  int bps = 0;
+  CK(occupancy(h->opts.precision, wpc, smem, &bps));
+  if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_device: kernel does not fit on an SM");
+  if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
+  int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
+  int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
+  CK(cudaMemsetAsync(h->d_counter, 0, 9 * sizeof(unsigned long long), s));
+  CK(launch_track(la, blocks, wpc, s));
+  h->last_blocks = blocks;
+  h->last_wpc = wpc;
+  return HC_OK;
+}
+
+int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, double t1_re, double t1_im,
+             double t0_re, double t0_im, hc_path_result* out_results, double* out_solutions, double* out_valuation,
+             double* out_last) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track: null handle");
+  if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track: call hc_set_homotopy first");
+  if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track: npaths < 0");
+  if (npaths == 0) return HC_OK;
+  if (!starts || !out_results || !out_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track: null buffer");
+  int n = h->prog.n;
+  int rc = ensure_capacity(h, npaths, n);
+  if (rc != HC_OK) return rc;
+  size_t nv = (size_t)npaths * n;
+  *h->h_cancel = 0;
+  CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  rc = hc_track_device(h, npaths, (const double*)h->d_starts, endgame, t1_re, t1_im, t0_re, t0_im, h->d_res,
+                       (double*)h->d_sol, h->d_val, (double*)h->d_last, nullptr);
+  if (rc != HC_OK) return rc;
+  CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)npaths * sizeof(hc_path_result), cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  if (out_valuation)
+    CK(cudaMemcpyAsync(out_valuation, h->d_val, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (out_last) CK(cudaMemcpyAsync(out_last, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long st[8];
+  CK(cudaMemcpyAsync(st, h->d_counter + 1, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < 8; ++i) h->stats[i] = (double)st[i];
+  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
+  return HC_OK;
+}
+
+int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t path_hi) {
+  if (!h || capacity < 0 || path_lo < 0 || path_hi < path_lo)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_log: bad argument");
+  if (capacity != h->log_cap) {
+    cudaFree(h->d_log);
+    h->d_log = nullptr;
+    h->log_cap = 0;
+    if (capacity > 0) CK(cudaMalloc(&h->d_log, (size_t)capacity * HC_LOG_FIELDS * sizeof(double)));
+    if (!h->d_log_count) CK(cudaMalloc(&h->d_log_count, sizeof(unsigned long long)));
+    h->log_cap = capacity;
+  }
+  h->log_lo = path_lo;
+  h->log_hi = path_hi;
+  return HC_OK;
+}
+
+int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_records) {
+  if (!h || !n_records || max_records < 0 || (max_records > 0 && !out))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_get_step_log: bad argument");
+  *n_records = 0;
+  if (h->log_cap == 0) return HC_OK;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, h->d_log_count, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  int64_t m = std::min<int64_t>((int64_t)std::min<unsigned long long>(cnt, (unsigned long long)h->log_cap), max_records);
+  if (m > 0) {
+    CK(cudaMemcpyAsync(out, h->d_log, (size_t)m * HC_LOG_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  *n_records = (int64_t)cnt;
+  return HC_OK;
+}
+
+int hc_cancel(hc_handle* h) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_cancel: null handle");
+  __atomic_store_n(h->h_cancel, 1, __ATOMIC_SEQ_CST);
+  return HC_OK;
+}
+
+const char* hc_last_error(hc_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> g(g_err_mu);
+  return g_err.c_str();
+}
+
+int hc_last_stats(hc_handle* h, double* out, int nout) {
+  if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
+  // [0] paths, [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double
+  // residuals, [4] Taylor orders (Σ K), [5] LU factorizations, [6] triangular solve pairs,
+  // [7] FP32 Taylor evaluations redone in FP64; derived: [8] monomials M, [9] value terms,
+  // [10] Jacobian terms, [11] blocks, [12] warps per block, [13] shared bytes per warp,
+  // [14] shared bytes of the CTA tables, [15] top-degree monomial offset
+  double all[16];
+  for (int i = 0; i < 8; ++i) all[i] = h->stats[i];
+  all[8] = h->prog.M;
+  all[9] = (double)h->prog.val_terms;
+  all[10] = (double)h->prog.jac_terms;
+  all[11] = h->last_blocks;
+  all[12] = h->last_wpc;
+  all[13] = h->layout.bytes;
+  all[14] = make_table_layout(h->prog, h->opts.precision).bytes;
+  all[15] = h->prog.top;
+  for (int i = 0; i < nout && i < 16; ++i) out[i] = all[i];
+  return HC_OK;
+}
+
+}  // extern "C"

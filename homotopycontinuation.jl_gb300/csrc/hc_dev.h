@@ -1,0 +1,82 @@
+// hc_dev.h — data shared by the host launcher and the path-tracking kernel.
+//
+// A homotopy is compiled on the host into a "monomial program" (the GPU counterpart of
+// ModelKit's InstructionSequence, src/model_kit/instruction_sequence.jl:1-27):
+//   * a monomial table in degree order; monomial m = monomial[parent] * x[var], m = 0 is 1,
+//   * "value rows": F_0..F_{n-1}, G_0..G_{n-1}; each a list of (coefficient, monomial),
+//   * "Jacobian rows": ∂F_i/∂x_j (row j*n+i) then ∂G_i/∂x_j (row n*n + j*n+i); a Jacobian
+//     term is (monomial, value term, exponent): its coefficient is exponent × the value term's,
+//     so the tables stay small enough to live in shared memory,
+// plus a static lane schedule: every row is cut into segments, segments are spread over the
+// 32 lanes of a warp, and each segment writes one partial sum ("slot"); slots of one row are
+// contiguous so the row total is a fixed-order sum.
+//
+// Shared memory of a CTA: [per-term tables, copied once per CTA][warp 0][warp 1]...
+#pragma once
+#include <cstdint>
+
+#include "../../include/hcgpu.h"
+
+namespace hcd {
+
+struct DevRows {
+  int nrows, nterms, nslots, nseg;
+  const int4* seg;      // [nseg] (row, term begin, term end, slot), grouped by lane
+  const int* lane_seg;  // [33]
+  const int* row_slot;  // [nrows + 1]
+};
+
+struct DevProg {
+  int n, M, nlev, top;  // top: first monomial of the highest degree level
+  const int2* mdef;     // [M] (parent, var)
+  const int* lev;       // [nlev + 1] monomial ranges per degree level (level 0 = {0})
+  DevRows val, jac;
+  // per-term tables (global copies; the kernel stages them in shared memory)
+  const double2* vcoef64;  // [val.nterms]
+  const float2* vcoef32;   // [val.nterms]
+  const uint16_t* vmono;   // [val.nterms]
+  const uint32_t* jcode;   // [jac.nterms] monomial | value-term << 16
+  // Jacobian segments carry their exponent multiplier in bits 24..31 of the slot field
+  double gamma_re, gamma_im;
+};
+
+// Byte offsets of the CTA tables and of the per-warp regions
+struct TableLayout {
+  int bytes;
+  int vcoef64, vcoef32, vmono, jcode, mdef;
+  int n64, n32, nmono, njcode, nmdef;  // sizes in bytes (multiples of 16)
+};
+struct WarpLayout {
+  int bytes;
+  int state, mono, part, A, LU, xJ, dinv, ipiv;
+  int vec;   // complex vectors (vn elements each, 16 B)
+  int rvec;  // real vectors (vn elements each, 8 B)
+  int vn;    // padded vector length (elements)
+};
+constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
+constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
+constexpr int HC_LOG_FIELDS = 20;  // doubles per step-log record
+
+struct Launch {
+  DevProg P;
+  hc_options O;
+  TableLayout T;
+  WarpLayout L;
+  int64_t npaths;
+  const double2* starts;
+  hc_path_result* res;
+  double2* sol;
+  double* val;
+  double2* last;
+  int mode;  // 1 endgame, 0 plain tracker
+  double t1_re, t1_im, t0_re, t0_im;
+  unsigned long long* counter;  // work queue head
+  volatile int* cancel;
+  unsigned long long* stats;  // [8] device counters
+  // optional step log: records of the paths in [log_lo, log_hi)
+  double* log;
+  unsigned long long* log_count;
+  long long log_cap, log_lo, log_hi;
+};
+
+}  // namespace hcd

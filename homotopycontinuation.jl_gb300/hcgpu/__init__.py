@@ -1,0 +1,39 @@
+"""hcgpu — GB300-native path tracking with the API of HomotopyContinuation.jl's
+total-degree hot path. See include/hcgpu.h for the C ABI."""
+from .systems import (
+    Poly,
+    System,
+    TotalDegreeHomotopy,
+    complex_gaussian,
+    cyclic,
+    dense_random_system,
+    monomials_upto,
+    random_gamma,
+    sparse_random_system,
+    total_degree_homotopy,
+    total_degree_start_solutions,
+    uneven_instances,
+    variables,
+)
+from .tracking import (
+    ENDGAME_CODES,
+    TRACKER_CODES,
+    EndgameOptions,
+    EndgameTracker,
+    PathResult,
+    Result,
+    Tracker,
+    TrackerOptions,
+    TrackerResult,
+    make_options,
+    multiplicities,
+    nat_infinity,
+    nfailed,
+    nnonsingular,
+    nsingular,
+    solve,
+    total_degree,
+    track,
+)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

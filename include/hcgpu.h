@@ -1,0 +1,155 @@
+/* hcgpu.h — C ABI of libhcgpu.so, a GB300 (sm_103a) path tracker for polynomial homotopy
+ * continuation with the semantics of HomotopyContinuation.jl's total-degree hot path.
+ *
+ * The reference tracks one path at a time inside Julia:
+ *   solve(F; start_system = :total_degree)            src/solve.jl:447-526
+ *     → total_degree_variables(F; gamma)               src/total_degree.jl:32-117
+ *     → threaded_solve: track(tracker, S[k])           src/solve.jl:628-709 (:669)
+ *       → EndgameTracker track!/step!                  src/endgame_tracker.jl:297-399, 902-914
+ *         → Tracker init!/step!                        src/tracker.jl:639-926
+ *     → PathResult / Result counts                     src/path_result.jl:76-98, src/result.jl:102-212
+ * This library replaces the per-path loop (serial_solve / threaded_solve, src/solve.jl:603-709)
+ * with one batched call: every path of the batch is tracked by one warp of a persistent CUDA
+ * kernel. Plain pointers and sizes only; the caller owns every host array it passes.
+ *
+ * Errors: every function returns an int status (HC_OK == 0). Per-path failures are not
+ * errors: they are return codes inside hc_path_result, with the values of
+ * EndgameTrackerCode (src/endgame_tracker.jl:100-117) or TrackerCode (src/tracker.jl:166-176).
+ */
+#ifndef HCGPU_H
+#define HCGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum hc_status {
+  HC_OK = 0,
+  HC_ERR_INVALID_ARG = 1,
+  HC_ERR_CUDA = 2,
+  HC_ERR_NO_SYSTEM = 3,
+  HC_ERR_CANCELLED = 4,
+  HC_ERR_UNSUPPORTED = 5,
+  HC_ERR_TOO_LARGE = 6
+};
+
+/* Arithmetic of the corrector, predictor and LU.
+ *   HC_PREC_FP64 : complex FP64 everywhere (the reference's arithmetic).
+ *   HC_PREC_MIXED: Jacobian, Taylor coefficients and LU in complex FP32; Newton residual,
+ *                  solution update, condition numbers and every threshold decision in FP64;
+ *                  double-double residuals on near-singular steps as in the reference. */
+enum hc_precision { HC_PREC_FP64 = 0, HC_PREC_MIXED = 1 };
+
+/* Step-size control. HC_STEP_PLAIN is update_stepsize! (src/tracker.jl:541-588).
+ * HC_STEP_LEARNED lets a loaded MLP propose the step length after each accepted step; any
+ * proposal the Newton contraction test rejects falls back to the plain rule. */
+enum hc_step_control { HC_STEP_PLAIN = 0, HC_STEP_LEARNED = 1 };
+
+/* Mirrors TrackerOptions + TrackerParameters (src/tracker.jl:45-140) and EndgameOptions
+ * (src/endgame_tracker.jl:47-72); hc_default_options fills in the reference defaults. */
+typedef struct hc_options {
+  int32_t max_steps;
+  int32_t extended_precision;
+  double max_step_size, max_initial_step_size, min_step_size, min_rel_step_size, terminate_cond;
+  double a, beta_a, beta_omega_p, beta_tau, strict_beta_tau;
+  int32_t min_newton_iters;
+  int32_t max_endgame_steps, max_endgame_extended_steps, max_winding_number;
+  int32_t zero_is_at_infinity, at_infinity_check, only_nonsingular, refine_steps;
+  double endgame_start, min_cond, min_cond_growth, min_coord_growth, singular_min_accuracy;
+  double val_finite_tol, val_at_infinity_tol, sing_cond, sing_accuracy, scaling_threshold;
+  /* GPU-side knobs (no counterpart in the reference) */
+  int32_t precision;      /* enum hc_precision */
+  int32_t step_control;   /* enum hc_step_control */
+  int32_t warps_per_cta;  /* 0 = autotuned */
+  int32_t ctas_per_sm;    /* 0 = as many as fit */
+} hc_options;
+
+/* Per-path record. Mirrors PathResult (src/path_result.jl:76-98) for endgame tracking and
+ * TrackerResult (src/tracker.jl:235-247) for plain tracking. */
+typedef struct hc_path_result {
+  int32_t return_code;     /* EndgameTrackerCode (endgame) / TrackerCode (plain) value */
+  int32_t winding_number;  /* 0 == nothing */
+  double t_re, t_im;       /* t where tracking stopped (0 on success with the endgame) */
+  double accuracy, residual, cond, omega, mu, tau;
+  int32_t singular, extended_precision, extended_precision_used, _pad;
+  int64_t accepted_steps, rejected_steps, steps_eg, path_number;
+  double last_t;           /* t of last_path_point */
+} hc_path_result;
+
+typedef struct hc_handle hc_handle;
+
+/* Fill *opts with the reference defaults (DEFAULT_TRACKER_PARAMETERS, EndgameOptions()). */
+int hc_default_options(hc_options* opts);
+
+/* Create a tracker on the current CUDA device. Replaces EndgameTracker(H; options)
+ * (src/endgame_tracker.jl:243-254). */
+int hc_create(const hc_options* opts, hc_handle** out);
+void hc_destroy(hc_handle* h);
+int hc_set_options(hc_handle* h, const hc_options* opts);
+
+/* Set the straight-line homotopy H(x,t) = γ t G(x) + (1-t) F(x)
+ * (src/homotopies/straight_line_homotopy.jl:10-68) from term tables:
+ *   *_eq[k]        equation of term k (0-based),
+ *   *_exps[k*n+j]  exponent of variable j in term k,
+ *   *_coef[2k..]   coefficient (re, im).
+ * For the total-degree start system G_i = s_i (x_i^{D_i} - 1) (src/total_degree.jl:62,102-106).
+ * n ≤ 32. Replaces the ModelKit compile step (src/model_kit/compiled_system_homotopy.jl:15-58):
+ * the tables become a monomial program evaluated by the kernel. */
+int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
+                    const double* G_coef, int nF, const int32_t* F_eq, const int32_t* F_exps,
+                    const double* F_coef, double gamma_re, double gamma_im);
+
+/* Track npaths start solutions (host arrays, npaths×n complex interleaved).
+ *   endgame = 1: EndgameTracker from t = t1_re to 0 (track(eg, x), src/endgame_tracker.jl:902-914),
+ *   endgame = 0: Tracker from t1 to t0 (track(tracker, x, t1, t0), src/tracker.jl:1023-1026).
+ * out_results[npaths], out_solutions[npaths×n complex]; out_valuation (npaths×n, may be NULL)
+ * receives val_x (src/valuation.jl:6-22); out_last (npaths×n complex, may be NULL) receives
+ * last_path_point with the endgame and val_tẋ (real parts) without it.
+ * Copies in, runs and copies out on the handle's stream; returns when the results are on the host. */
+int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, double t1_re,
+             double t1_im, double t0_re, double t0_im, hc_path_result* out_results,
+             double* out_solutions, double* out_valuation, double* out_last);
+
+/* Same, on device pointers, asynchronous on `stream` (a cudaStream_t, or NULL for the
+ * handle's stream). No host synchronisation; the caller synchronises the stream. */
+int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int endgame,
+                    double t1_re, double t1_im, double t0_re, double t0_im,
+                    hc_path_result* d_results, double* d_solutions, double* d_valuation,
+                    double* d_last, void* stream);
+
+/* Request cancellation of a running hc_track on this handle (thread-safe). Paths not yet
+ * finished report TrackerCode terminated_unknown and hc_track returns HC_ERR_CANCELLED. */
+int hc_cancel(hc_handle* h);
+
+/* Last error message of this handle (or of the library when h is NULL). */
+const char* hc_last_error(hc_handle* h);
+
+/* Device work counters of the last call: kernel launches, evaluations, LU factorizations,
+ * and the algorithmic FP64/FP32 flop counts used for the roofline (out[0..7]). */
+int hc_last_stats(hc_handle* h, double* out, int nout);
+
+/* Step log: after this call, every step attempted on a path whose 0-based index lies in
+ * [path_lo, path_hi) appends one record of HC_STEP_LOG_FIELDS doubles to a device buffer of
+ * `capacity` records (capacity 0 disables logging). The fields follow the reference's
+ * PathInfo trace (src/path_info.jl:3-21): path number, t (re, im), Δs tried, trust region,
+ * local error, ω, μ (before the step), accepted, Newton iterations, θ, ‖Δx₀‖, ‖x‖∞,
+ * previous Δs, next Δs, flags (extended precision | FP64-fallback << 1 | Newton code << 2),
+ * ω and accuracy returned by the corrector, trust region after the step, accepted steps.
+ * It is the training data of the learned step proposal. */
+#define HC_STEP_LOG_FIELDS 20
+int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t path_hi);
+/* Copy up to max_records records of the last call to `out`; *n_records receives the number
+ * of records the call produced (which may exceed the capacity). */
+int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_records);
+
+/* FP64 and FP32 CUDA-core FMA throughput of the current GPU in TFLOP/s, measured by a
+ * short microbenchmark: the roofline denominators of this FP-pipe-bound path. No
+ * counterpart in the reference. */
+int hc_fma_peak(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HCGPU_H */
