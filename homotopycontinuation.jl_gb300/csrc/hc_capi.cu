@@ -324,7 +324,7 @@ struct hc_handle {
   unsigned long long* d_counter = nullptr;  // [1 + 8 stats]
   int* h_cancel = nullptr;                  // mapped host memory
   int* d_cancel = nullptr;
-  double stats[8] = {0};
+  double stats[9] = {0};
   int last_blocks = 0, last_wpc = 0;
   // step log
   double* d_log = nullptr;
@@ -400,7 +400,7 @@ int hc_create(const hc_options* opts, hc_handle** out) {
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, 9 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, 10 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaHostAlloc(&h->h_cancel, sizeof(int), cudaHostAllocMapped);
   if (e == cudaSuccess) {
     *h->h_cancel = 0;
@@ -595,7 +595,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
-  CK(cudaMemsetAsync(h->d_counter, 0, 9 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(h->d_counter, 0, 10 * sizeof(unsigned long long), s));
   CK(launch_track(la, blocks, wpc, s));
   h->last_blocks = blocks;
   h->last_wpc = wpc;
@@ -625,10 +625,10 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   if (out_valuation)
     CK(cudaMemcpyAsync(out_valuation, h->d_val, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (out_last) CK(cudaMemcpyAsync(out_last, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-  unsigned long long st[8];
-  CK(cudaMemcpyAsync(st, h->d_counter + 1, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long st[9];
+  CK(cudaMemcpyAsync(st, h->d_counter + 1, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < 8; ++i) h->stats[i] = (double)st[i];
+  for (int i = 0; i < 9; ++i) h->stats[i] = (double)st[i];
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
   return HC_OK;
 }
@@ -682,20 +682,21 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
   // [0] paths, [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double
   // residuals, [4] Taylor orders (Σ K), [5] LU factorizations, [6] triangular solve pairs,
-  // [7] FP32 Taylor evaluations redone in FP64; derived: [8] monomials M, [9] value terms,
-  // [10] Jacobian terms, [11] blocks, [12] warps per block, [13] shared bytes per warp,
-  // [14] shared bytes of the CTA tables, [15] top-degree monomial offset
-  double all[16];
-  for (int i = 0; i < 8; ++i) all[i] = h->stats[i];
-  all[8] = h->prog.M;
-  all[9] = (double)h->prog.val_terms;
-  all[10] = (double)h->prog.jac_terms;
-  all[11] = h->last_blocks;
-  all[12] = h->last_wpc;
-  all[13] = h->layout.bytes;
-  all[14] = make_table_layout(h->prog, h->opts.precision).bytes;
-  all[15] = h->prog.top;
-  for (int i = 0; i < nout && i < 16; ++i) out[i] = all[i];
+  // [7] FP32 Taylor evaluations redone in FP64, [8] paths moved to FP64 (mixed precision);
+  // derived: [9] monomials M, [10] value terms, [11] Jacobian terms, [12] blocks, [13] warps
+  // per block, [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree
+  // monomial offset
+  double all[17];
+  for (int i = 0; i < 9; ++i) all[i] = h->stats[i];
+  all[9] = h->prog.M;
+  all[10] = (double)h->prog.val_terms;
+  all[11] = (double)h->prog.jac_terms;
+  all[12] = h->last_blocks;
+  all[13] = h->last_wpc;
+  all[14] = h->layout.bytes;
+  all[15] = make_table_layout(h->prog, h->opts.precision).bytes;
+  all[16] = h->prog.top;
+  for (int i = 0; i < nout && i < 17; ++i) out[i] = all[i];
   return HC_OK;
 }
 

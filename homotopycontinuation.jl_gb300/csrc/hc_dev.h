@@ -72,7 +72,7 @@ struct Launch {
   double t1_re, t1_im, t0_re, t0_im;
   unsigned long long* counter;  // work queue head
   volatile int* cancel;
-  unsigned long long* stats;  // [8] device counters
+  unsigned long long* stats;  // [9] device counters
   // optional step log: records of the paths in [log_lo, log_hi)
   double* log;
   unsigned long long* log_count;

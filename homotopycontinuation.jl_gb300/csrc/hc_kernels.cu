@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
     atomicAdd(la.stats + 5, T->c_lu);
     atomicAdd(la.stats + 6, T->c_solve);
     atomicAdd(la.stats + 7, T->c_taylor64);
+    atomicAdd(la.stats + 8, T->c_switch64);
   }
 }
 

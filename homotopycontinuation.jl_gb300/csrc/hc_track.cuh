@@ -165,6 +165,8 @@ struct PathTracker {
   bool factorized, scaled;
   int Aprec;  // 64 or 32: arithmetic of the current A / LU
   bool j64;   // mixed precision only: this path fell back to an FP64 Jacobian
+  bool omega_reseed;  // mixed precision: take ω from the first FP64 correction after the switch
+  double pred_delta;  // relative correction of the last ẋ refinement step (≈ FP32 solve error)
   c64 tJ;     // t of the last Jacobian evaluation (its x is xJ)
 
   // ---- Predictor state (src/predictor.jl:72-103)
@@ -204,7 +206,7 @@ struct PathTracker {
   long long cur_path;
 
   // ---- counters
-  unsigned long long c_evalj, c_eval, c_evaldd, c_taylor, c_lu, c_solve, c_taylor64;
+  unsigned long long c_evalj, c_eval, c_evaldd, c_taylor, c_lu, c_solve, c_taylor64, c_switch64;
 
   // all 32 lanes call init with the same arguments (the object is one per warp, in shared memory)
   __device__ void init(const Launch* la, char* base, char* tbase) {
@@ -271,7 +273,7 @@ struct PathTracker {
     factorized = scaled = false;
     Aprec = 64;
     j64 = false;
-    c_evalj = c_eval = c_evaldd = c_taylor = c_lu = c_solve = c_taylor64 = 0;
+    c_evalj = c_eval = c_evaldd = c_taylor = c_lu = c_solve = c_taylor64 = c_switch64 = 0;
     ca = O->a;
     ch_a = h_fn(ca);
     k_sq12ha = sqrt(1 - 2 * ch_a);
@@ -1097,6 +1099,7 @@ struct PathTracker {
       c64 xt = jac_ldiv(ul, nullptr);
       double delta = fp_refine_step(xt, ul, w);
       cond_H_xd = delta / EPS;
+      pred_delta = delta;
       if (lu32) {
         if (!(delta <= 1e-2)) {
           j64 = true;
@@ -1473,6 +1476,8 @@ struct PathTracker {
   // init! (:639-754); returns is_tracking
   __device__ HC_NI bool tracker_init(c64 t1, c64 t0) {
     j64 = false;
+    omega_reseed = false;
+    pred_delta = 0.0;
     ss.init(t1, t0);
     Ds_prev = 0.0;
     accuracy = EPS;
@@ -1548,17 +1553,21 @@ struct PathTracker {
     predict(t, Dt);
     norm_update(ld(xh));
     NewtonResult res;
+    if (MIXED && !j64 && (ss.Ds() < 1e-6 * fast_abs(t) || pred_delta > 1e-3)) {
+      // With an FP32 Jacobian Newton contracts only linearly (κ ≈ cond(J)·2^-23); the
+      // quadratic model behind ω = 2‖Δx₁‖/‖Δx₀‖² then reads κ as curvature, ω grows as the
+      // steps shrink and the steps shrink as ω grows. A tiny step relative to t, or a
+      // predictor solve error δ ≈ κ above 1e-3, moves the path to FP64 for good.
+      switch_to_fp64(t);
+      predict(t, Dt);
+    }
     if (MIXED && !j64) {
       res = newton<c32>(xb, xh, tp, mu, omega, extended_prec, false, accepted_steps == 0);
       if (res.code != NEWT_CONVERGED) {
         // The FP32 Jacobian could not carry the correction: switch the path to FP64, redo the
         // predictor at the accepted point (its FP32 coefficients may be the culprit) and
         // retry this step with the same step size.
-        j64 = true;
-        H_eval_jac<c64>(x, t);
-        updated();
-        predictor_compute(t, local_error);
-        tau = trust_region;
+        switch_to_fp64(t);
         predict(t, Dt);
         res = newton<c64>(xb, xh, tp, mu, omega, extended_prec, false, accepted_steps == 0);
       }
@@ -1573,7 +1582,12 @@ struct PathTracker {
       accuracy = res.accuracy;
       mu = jmax(res.accuracy, EPS);
       omega_prev = omega;
-      omega = jmax(jmax(res.omega, 0.5 * omega), 0.1);
+      if (MIXED && omega_reseed) {
+        omega = jmax(res.omega, 0.1);
+        omega_reseed = false;
+      } else {
+        omega = jmax(jmax(res.omega, 0.5 * omega), 0.1);
+      }
       update_precision(res.mu_low);
       if (ss.is_done() && O->extended_precision && accuracy > 1e-14) {
         accuracy = refine_current_solution(1e-14, 3);
@@ -1627,6 +1641,17 @@ struct PathTracker {
       default: break;
     }
     if (LANE < HC_LOG_FIELDS) rec[LANE] = v;
+  }
+  // mixed precision: continue this path with an FP64 Jacobian, Taylor series and LU; the
+  // predictor is recomputed at the accepted point and ω re-estimated by the next correction
+  __device__ HC_NI void switch_to_fp64(c64 t) {
+    j64 = true;
+    omega_reseed = true;
+    ++c_switch64;
+    H_eval_jac<c64>(x, t);
+    updated();
+    predictor_compute(t, local_error);
+    tau = trust_region;
   }
   // LA.cond(tracker, x, t, d_l, d_r) (src/tracker.jl:509-514), in FP64
   __device__ HC_NI double tracker_cond(const c64* xv, c64 t, const double* dl, const double* dr) {

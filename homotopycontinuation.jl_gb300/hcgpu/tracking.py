@@ -231,12 +231,12 @@ class _Handle:
         return out[: min(int(cnt[0]), int(max_records))]
 
     STAT_NAMES = ["paths", "evals_jac", "evals", "evals_dd", "taylor_orders", "lu", "solves", "taylor_fp64_redo",
-                  "monomials", "value_terms", "jacobian_terms", "blocks", "warps_per_block", "smem_per_warp",
-                  "smem_tables", "top"]
+                  "paths_to_fp64", "monomials", "value_terms", "jacobian_terms", "blocks", "warps_per_block",
+                  "smem_per_warp", "smem_tables", "top"]
 
     def stats(self):
-        out = np.zeros(16)
-        _lib.check(self.L.hc_last_stats(self.h, _lib.ptr(out), 16), self.h)
+        out = np.zeros(17)
+        _lib.check(self.L.hc_last_stats(self.h, _lib.ptr(out), 17), self.h)
         return dict(zip(self.STAT_NAMES, out.tolist()))
 
     def cancel(self):
