@@ -1,0 +1,350 @@
+"""Benchmark: paths/sec of the GB300 path tracker on the 10×10 dense-cubic total-degree
+homotopy (59,049 paths), with the plain FP64 GPU tracker and the CPU oracle beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A "step" is one batched tracking call over all paths of the workload. Prints one JSON line.
+Under torchrun (N > 1) every rank tracks its own seeded instance (weak scaling) and rank 0
+prints the aggregate. --impl reference times the reference algorithm on the host CPU: the
+HomotopyContinuation.jl package itself needs Julia, which is not installed, so the CPU leg is
+the C++ restatement in oracle/ (kind "port") on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as ct
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "homotopycontinuation.jl_gb300"))
+
+METRIC = "paths/sec at ≤1e-10 rel endpoint err: learned vs plain step control, 1 GB300"
+N_VARS, DEGREE = 10, 3
+WORKLOAD = "total-degree homotopy, 10 dense cubics in 10 complex variables (286 monomials each), 59,049 paths"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--step-control", default="plain", choices=["plain", "learned"])
+    p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def workload(seed):
+    import hcgpu as hc
+
+    F, g = hc.dense_random_system(N_VARS, DEGREE, seed=seed)
+    H = hc.total_degree_homotopy(F, g)
+    S = hc.total_degree_start_solutions(H.degrees)
+    return H, S
+
+
+def flop_model(stats, n, precision):
+    """Algorithmic FP64 / FP32 flops of one call from the device counters and the program
+    census (complex multiply 6, complex multiply-add 8, complex add 2 flops)."""
+    M, Tv, Tj = stats["monomials"], stats["value_terms"], stats["jacobian_terms"]
+    mono = 6 * M
+    val = 8 * Tv + 14 * 2 * n
+    jac = 8 * Tj + 14 * n * n
+    lu = 8 * sum((n - k - 1) ** 2 for k in range(n)) + 6 * n * (n - 1) / 2 + 10 * n
+    solve = 16 * n * n
+    taylor_per_order = 6 * M * 4 + 16 * Tv  # series (≤4 products per monomial) + two row orders
+    dd = 84 * (Tv + M)
+    f64 = (stats["evals_jac"] * (mono + val) + stats["evals"] * (mono + val) + stats["evals_dd"] * dd)
+    f32 = 0.0
+    jac_lu = stats["evals_jac"] * jac + stats["lu"] * lu + stats["solves"] * solve
+    tay = stats["taylor_orders"] / 2.0 * taylor_per_order
+    if precision == "mixed":
+        f32 += jac_lu + tay
+        f64 += stats["taylor_fp64_redo"] * taylor_per_order
+    else:
+        f64 += jac_lu + tay
+    return f64, f32
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(mhz)) if mhz else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def cpu_baseline(H, S, sample, nthreads=0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import hco
+
+    cores = nthreads or os.cpu_count()
+    idx = np.linspace(0, len(S) - 1, sample).astype(np.int64)
+    t = time.perf_counter()
+    res, xs, _, _ = hco.track(H.G.term_arrays(), H.F.term_arrays(), H.gamma, S[idx], nthreads=cores)
+    dt = time.perf_counter() - t
+    return {"value": sample / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+            "sample": f"{sample} of {len(S)} paths (evenly spaced indices) of the same homotopy, C++ FP64 "
+                      f"restatement of the reference EndgameTracker on {cores} threads, {dt:.1f} s"}, idx, xs, res
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host CPU (oracle port, all threads)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    H, S = workload(args.seed)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import hco
+
+    hco.build()
+    cores = os.cpu_count()
+    sample = min(args.cpu_sample, len(S))
+    idx = np.linspace(0, len(S) - 1, sample).astype(np.int64)
+    St = S[idx]
+    for _ in range(args.warmup):
+        hco.track(H.G.term_arrays(), H.F.term_arrays(), H.gamma, St[: max(64, sample // 8)], nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        hco.track(H.G.term_arrays(), H.F.term_arrays(), H.gamma, St, nthreads=cores)
+        times.append(time.perf_counter() - t)
+    ms = 1000 * float(np.mean(times))
+    value = sample / (ms / 1000)
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded complex Gaussian coefficients)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "seed": args.seed, "sample_paths": sample},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} evenly spaced paths of {len(S)} per step; HomotopyContinuation.jl needs "
+                                   f"Julia (not installed), so the C++ restatement of its tracker runs instead"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import hcgpu as hc
+    from hcgpu import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    H, S = workload(args.seed + rank)
+    npaths, n = S.shape
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)  # a real stream: the kernel and its events share it
+    torch.cuda.set_stream(stream)
+    d_starts = torch.from_numpy(np.ascontiguousarray(S).view(np.float64).reshape(-1)).to(dev)
+    d_res = torch.empty(npaths * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    d_sol = torch.empty(npaths * n * 2, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    L = _lib.load()
+
+    def tracker(precision, step_control):
+        to = hc.TrackerOptions(precision=precision, step_control=step_control)
+        return hc.EndgameTracker(H, to)
+
+    def device_call(T):
+        rc = L.hc_track_device(T._h.h, npaths, ct.c_void_p(d_starts.data_ptr()), 1, 1.0, 0.0, 0.0, 0.0,
+                               ct.c_void_p(d_res.data_ptr()), ct.c_void_p(d_sol.data_ptr()), None, None,
+                               ct.c_void_p(stream.cuda_stream))
+        _lib.check(rc, T._h.h)
+
+    def timed(T, steps, warmup):
+        for _ in range(warmup):
+            device_call(T)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(steps):
+            flush_l2(flush)
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            h0 = time.perf_counter()
+            e0.record(stream)
+            device_call(T)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            host_ms = 1000 * (time.perf_counter() - h0)
+            dev_ms = e0.elapsed_time(e1)
+            if not (0.8 * host_ms <= dev_ms <= 1.05 * host_ms + 1.0):
+                raise RuntimeError(f"device timing {dev_ms:.3f} ms disagrees with host timing {host_ms:.3f} ms")
+            times.append(dev_ms)
+        return times
+
+    fp64_peak, fp32_peak = _lib.fma_peak()
+    T = tracker(args.precision, args.step_control)
+    with ClockSampler(local) as clk:
+        times = timed(T, args.steps, args.warmup)
+    stats = T.stats()
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+    sol = d_sol.cpu().numpy().view(np.complex128).reshape(npaths, n)
+    ms = float(np.mean(times))
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * npaths / (ms_max / 1000)
+
+    # plain FP64 GPU tracker on the same paths (the ratio's denominator) and endpoint check
+    T64 = tracker("fp64", "plain")
+    t64 = timed(T64, 1, 1)
+    res64 = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+    sol64 = d_sol.cpu().numpy().view(np.complex128).reshape(npaths, n)
+    both = (res["return_code"] == 1) & (res64["return_code"] == 1) & (res["singular"] == 0) & (res64["singular"] == 0)
+    rel = np.abs(sol[both] - sol64[both]).max(1) / np.abs(sol64[both]).max(1)
+    counts = lambda r: {"nonsingular": int(((r["return_code"] == 1) & (r["singular"] == 0)).sum()),
+                        "singular": int(((r["return_code"] == 1) & (r["singular"] == 1)).sum()),
+                        "at_infinity": int(np.isin(r["return_code"], [2, 3]).sum()),
+                        "failed": int((~np.isin(r["return_code"], [1, 2, 3])).sum())}
+
+    # end to end through the public host API: host arrays in, host results out
+    e2e_steps = max(1, min(args.steps, 3))
+    out_res = np.zeros(npaths, dtype=_lib.RESULT_DTYPE)
+    out_sol = np.zeros((npaths, n), dtype=np.complex128)
+    pinned = torch.from_numpy(np.ascontiguousarray(S).view(np.float64).reshape(-1)).pin_memory()
+    starts_np = pinned.numpy()
+    e2e_times = []
+    for _ in range(e2e_steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.hc_track(T._h.h, npaths, starts_np.ctypes.data_as(ct.c_void_p), 1, 1.0, 0.0, 0.0, 0.0,
+                        out_res.ctypes.data_as(ct.c_void_p), out_sol.ctypes.data_as(ct.c_void_p), None, None)
+        _lib.check(rc, T._h.h)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * npaths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(S.nbytes),
+           "d2h_bytes_per_step": int(out_res.nbytes + out_sol.nbytes)}
+
+    f64, f32 = flop_model(stats, n, args.precision)
+    dur_s = ms / 1000
+    ach64 = f64 / dur_s / 1e12
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu, idx, xo, ro = cpu_baseline(H, S, min(args.cpu_sample, npaths))
+        okc = (ro["return_code"] == 1) & (res["return_code"][idx] == 1)
+        rel_oracle = float((np.abs(sol[idx][okc] - xo[okc]).max(1) / np.abs(xo[okc]).max(1)).max()) if okc.any() else None
+        codes_equal = bool((ro["return_code"] == res["return_code"][idx]).all())
+    else:
+        rel_oracle, codes_equal = None, None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": "synthetic (seeded complex Gaussian coefficients, N(0,1/2) re/im)",
+            "config": {"workload": WORKLOAD, "seed": args.seed, "paths_per_gpu": npaths, "n": n, "degree": DEGREE,
+                       "precision": args.precision, "step_control": args.step_control,
+                       "l2": "256 MiB buffer written between timed steps (inputs are smaller than L2)",
+                       "parallelism": f"weak: one seeded instance per GPU x{world}",
+                       "warps_per_cta": stats["warps_per_block"], "ctas": stats["blocks"]},
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "roofline": {"bound": "fp64", "achieved": ach64, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": ach64 / fp64_peak, "traffic": None,
+                         "peak_source": "measured FP64 FMA microbenchmark (hc_fma_peak) on this GPU",
+                         "fp32_achieved": f32 / dur_s / 1e12, "fp32_peak": fp32_peak,
+                         "flops_fp64_per_launch": f64, "flops_fp32_per_launch": f32},
+            "cpu_baseline": cpu,
+            "plain_fp64_gpu": {"value": npaths / (float(np.mean(t64)) / 1000), "unit": "paths/s",
+                               "counts": counts(res64)},
+            "speedup_vs_plain_fp64_gpu": (npaths / dur_s) / (npaths / (float(np.mean(t64)) / 1000)),
+            "counts": counts(res),
+            "counts_identical_to_fp64": counts(res) == counts(res64),
+            "max_rel_endpoint_err_vs_fp64_gpu": float(rel.max()) if len(rel) else None,
+            "max_rel_endpoint_err_vs_oracle_sample": rel_oracle,
+            "codes_identical_to_oracle_sample": codes_equal,
+            "device_counters": {k: stats[k] for k in ["evals_jac", "evals", "evals_dd", "taylor_orders", "lu",
+                                                     "solves", "taylor_fp64_redo", "paths_to_fp64"]},
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

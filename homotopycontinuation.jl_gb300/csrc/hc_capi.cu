@@ -326,6 +326,7 @@ struct hc_handle {
   int* d_cancel = nullptr;
   double stats[9] = {0};
   int last_blocks = 0, last_wpc = 0;
+  cudaStream_t last_stream = nullptr;
   // step log
   double* d_log = nullptr;
   unsigned long long* d_log_count = nullptr;
@@ -599,6 +600,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   CK(launch_track(la, blocks, wpc, s));
   h->last_blocks = blocks;
   h->last_wpc = wpc;
+  h->last_stream = s;
   return HC_OK;
 }
 
@@ -680,6 +682,12 @@ const char* hc_last_error(hc_handle* h) {
 
 int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
+  if (h->last_blocks > 0) {  // counters of the last call (hc_track or hc_track_device) on this handle
+    unsigned long long st[9];
+    CK(cudaMemcpyAsync(st, h->d_counter + 1, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->last_stream));
+    CK(cudaStreamSynchronize(h->last_stream));
+    for (int i = 0; i < 9; ++i) h->stats[i] = (double)st[i];
+  }
   // [0] paths, [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double
   // residuals, [4] Taylor orders (Σ K), [5] LU factorizations, [6] triangular solve pairs,
   // [7] FP32 Taylor evaluations redone in FP64, [8] paths moved to FP64 (mixed precision);
@@ -701,3 +709,4 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
 }
 
 }  // extern "C"
+

@@ -1,0 +1,28 @@
+"""Known-answer systems of the reference test suite (tests/golden/kat_systems.json)."""
+import json
+import os
+
+import numpy as np
+
+import hcgpu as hc
+
+_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "kat_systems.json")
+KAT = json.load(open(_PATH))
+
+
+def system(name):
+    d = KAT[name]
+    return hc.System([np.array(e, dtype=np.int32) for e in d["exponents"]],
+                     [np.array([complex(*c) for c in cs]) for cs in d["coefficients"]], nvars=d["n"])
+
+
+def gamma(name):
+    return complex(*KAT[name]["gamma"])
+
+
+def winding_family(d):
+    a = KAT["winding_family_a"]
+    x, y = hc.variables(2)
+    f1 = (a[0] * x**d + a[1] * y) * (a[2] * x + a[3] * y) + 1
+    f2 = (a[0] * x**d + a[1] * y) * (a[4] * x + a[5] * y) + 1
+    return hc.System.from_polys([f1, f2])

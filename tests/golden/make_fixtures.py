@@ -1,0 +1,96 @@
+"""Generate tests/golden/kat_systems.json from HomotopyContinuation.jl's own test files.
+
+The known-answer systems, fixed γ values and expected counts of the reference's endgame,
+EndgameTracker and valuation tests are read as text from the reference checkout and turned
+into term tables (exponent rows + complex coefficients). Run in a container that has the
+reference sources:
+
+    python tests/golden/make_fixtures.py [/path/to/HomotopyContinuation.jl]
+
+The JSON is committed; the tests never read the reference checkout.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "homotopycontinuation.jl_gb300"))
+
+from hcgpu.systems import Poly, System, variables  # noqa: E402
+
+
+def julia_to_python(expr: str) -> str:
+    e = expr.replace("\n", " ")
+    e = e.replace("^", "**")
+    e = re.sub(r"(\d)([a-zA-Z(])", r"\1*\2", e)  # implicit multiplication 3x, 2(, 1.3im
+    e = re.sub(r"\bim\b", "1j", e)
+    return e
+
+
+def to_system(exprs, names):
+    vs = variables(len(names))
+    env = dict(zip(names, vs))
+    polys = [eval(julia_to_python(e), {}, env) for e in exprs]
+    polys = [p if isinstance(p, Poly) else Poly.const(p, len(names)) for p in polys]
+    S = System.from_polys(polys)
+    return {"n": S.n, "exponents": [e.tolist() for e in S.exponents],
+            "coefficients": [[[c.real, c.imag] for c in cs] for cs in S.coefficients]}
+
+
+def split_top_level(s: str):
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur)
+    return [o.strip() for o in out if o.strip()]
+
+
+def main(ref):
+    test = os.path.join(ref, "test")
+    eg = open(os.path.join(test, "endgame_tracker_test.jl")).read()
+    en = open(os.path.join(test, "endgame_test.jl")).read()
+    val = open(os.path.join(test, "valuation_test.jl")).read()
+    out = {"source": "HomotopyContinuation.jl test/endgame_tracker_test.jl, test/endgame_test.jl, test/valuation_test.jl"}
+
+    # EndgameTracker test: 2×2 quadrics, γ = 1.3im + 0.4
+    m = re.search(r"f = \[(2\.3 \* x\^2.*?)\]\n\s*tracker, starts = total_degree\(System\(f\); gamma = ([^)]*)\)", eg)
+    out["quadrics_2x2"] = {**to_system(split_top_level(m.group(1)), ["x", "y"]),
+                           "gamma": list(map(float, [complex(eval(julia_to_python(m.group(2)))).real,
+                                                      complex(eval(julia_to_python(m.group(2)))).imag])),
+                           "expect": {"codes": ["success", "success", "at_infinity", "at_infinity"],
+                                      "valuation_at_infinity": [-1.0, -1.0]}}
+    # winding number family a-coefficients
+    m = re.search(r'Winding Number Family.*?a = \[([^\]]*)\]', en, re.S)
+    a = [float(v) for v in m.group(1).split(",")]
+    out["winding_family_a"] = a
+    # Mohab system + fixed γ; the reference orders the variables as System(F, [x, z, y])
+    blk = en[en.index('@testset "Mohab"'):]
+    m = re.search(r"F = \[(.*?)\n\s*\]\n", blk, re.S)
+    eqs = split_top_level(m.group(1))
+    g = re.search(r"γ = ([-0-9.e]+) \+ ([0-9.e]+)im", blk)
+    out["mohab"] = {**to_system(eqs, ["x", "z", "y"]), "gamma": [float(g.group(1)), float(g.group(2))],
+                    "expect": {"nnonsingular": int(re.search(r"nnonsingular\(res\) == (\d+)", blk).group(1))}}
+    # cyclic-7 expected count
+    out["cyclic7"] = {"expect": {"nsolutions": int(re.search(r"cyclic\(7\).*?nsolutions\(res\) == (\d+)", en, re.S).group(1))}}
+    # valuation example 3 (endgame side) system and targets
+    m = re.search(r'Example 3.*?a = \[([^\]]*)\]', val, re.S)
+    out["valuation_example3_a"] = [float(v) for v in m.group(1).split(",")]
+    with open(os.path.join(HERE, "kat_systems.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(HERE, "kat_systems.json"))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

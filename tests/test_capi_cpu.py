@@ -1,0 +1,156 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports every symbol of
+include/hcgpu.h, its structs match the header's layout, defaults mirror the reference, and
+argument errors come back as status codes."""
+import ctypes as ct
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import hcgpu as hc
+from hcgpu import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hcgpu.h")
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(hc_\w+)\(", txt, re.M)))
+
+
+def test_library_exports_header_symbols():
+    L = _lib.load()
+    names = header_functions()
+    assert len(names) >= 10
+    for nm in names:
+        assert hasattr(L, nm), nm
+    assert set(_lib.EXPORTS) == set(names)
+
+
+def test_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "hcgpu.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(hc_options), sizeof(hc_path_result),"
+        " offsetof(hc_options, precision), offsetof(hc_path_result, accepted_steps),"
+        " offsetof(hc_path_result, last_t));return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    so, sr, op, oa, ol = map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split())
+    assert so == ct.sizeof(_lib.Options)
+    assert sr == _lib.RESULT_DTYPE.itemsize
+    assert op == _lib.Options.precision.offset
+    assert oa == _lib.RESULT_DTYPE.fields["accepted_steps"][1]
+    assert ol == _lib.RESULT_DTYPE.fields["last_t"][1]
+
+
+def test_default_options_mirror_reference():
+    o = _lib.default_options()
+    # src/tracker.jl:45-62, :105-140 and src/endgame_tracker.jl:47-72
+    assert (o.a, o.beta_a, o.beta_omega_p, o.beta_tau, o.strict_beta_tau, o.min_newton_iters) == (0.125, 1.0, 3.0, 0.4, 0.3, 2)
+    assert (o.max_steps, o.extended_precision, o.min_step_size, o.terminate_cond) == (10000, 1, 1e-48, 1e13)
+    assert (o.endgame_start, o.max_endgame_steps, o.max_endgame_extended_steps) == (0.1, 2000, 400)
+    assert (o.min_cond, o.min_cond_growth, o.min_coord_growth, o.max_winding_number) == (1e6, 1e4, 100.0, 6)
+    assert (o.val_finite_tol, o.val_at_infinity_tol, o.sing_cond, o.sing_accuracy) == (0.05, 0.01, 1e14, 1e-12)
+    assert (o.singular_min_accuracy, o.scaling_threshold, o.refine_steps) == (1e-6, -30.0, 3)
+    opts = hc.make_options(hc.TrackerOptions(parameters="conservative"))
+    assert (opts.beta_omega_p, opts.beta_tau, opts.strict_beta_tau) == (4.0, 0.25, 0.1875)
+
+
+def test_argument_errors_are_status_codes():
+    L = _lib.load()
+    assert L.hc_create(None, None) == 1
+    assert L.hc_track(None, 1, None, 1, 1.0, 0.0, 0.0, 0.0, None, None, None, None) == 1
+    assert L.hc_set_step_log(None, 10, 0, 1) == 1
+    assert L.hc_last_error(None)
+    o = _lib.default_options()
+    h = ct.c_void_p()
+    rc = L.hc_create(ct.byref(o), ct.byref(h))
+    if rc == 0:  # a GPU is present: exercise the argument checks of a live handle
+        assert L.hc_track(h, 4, None, 1, 1.0, 0.0, 0.0, 0.0, None, None, None, None) == 3  # no system yet
+        assert L.hc_set_homotopy(h, 0, 0, None, None, None, 0, None, None, None, 1.0, 0.0) == 5
+        L.hc_destroy(h)
+    else:
+        assert rc == 2 and b"hc_create" in L.hc_last_error(None)
+
+
+def test_start_solutions_order():
+    # src/total_degree.jl:240-262: product order with the first index fastest
+    S = hc.total_degree_start_solutions([2, 3])
+    assert S.shape == (6, 2)
+    np.testing.assert_allclose(S[:, 0], [1, -1, 1, -1, 1, -1], atol=1e-15)
+    np.testing.assert_allclose(S[:, 1], np.repeat(np.exp(2j * np.pi * np.arange(3) / 3), 2), atol=1e-15)
+
+
+def test_total_degree_homotopy_scaling():
+    F, g = hc.dense_random_system(3, 2, seed=4)
+    H = hc.total_degree_homotopy(F, g)
+    assert H.degrees == [2, 2, 2] and H.bezout_number() == 8
+    for i in range(3):
+        assert np.isclose(H.scaling[i], np.abs(F.coefficients[i]).max())
+        x = np.array([0.3, -0.2 + 0.1j, 1.1])
+        assert np.isclose(H.G.evaluate(x)[i], H.scaling[i] * (x[i] ** 2 - 1))
+
+
+def test_multiplicities_and_counts():
+    # src/unique_points.jl:314-341 and src/result.jl:161-212
+    mk = lambda code, sol, sing, k: hc.PathResult(code, np.array(sol, complex), 0.0, 1e-14, 1e-14, sing, 1.0, None,
+                                                   False, k, None, (None, 0.0), None, 1.0, 1e-16, 10, 0, 0, False)
+    prs = [mk("success", [1, 2], False, 1), mk("success", [3, 3], True, 2), mk("success", [3, 3 + 1e-12], True, 3),
+           mk("at_infinity", [1e9, 0], False, 4), mk("terminated_max_steps", [0, 0], False, 5)]
+    R = hc.Result(prs)
+    assert hc.nnonsingular(R) == 1 and hc.nat_infinity(R) == 1 and hc.nfailed(R) == 1
+    assert hc.nsingular(R) == 1 and hc.nsingular(R, counting_multiplicities=True) == 2
+    assert prs[1].multiplicity == 2
+
+
+def test_shard_ranges_cover_batch():
+    from hcgpu.parallel import shard_range
+
+    for npaths in [0, 1, 7, 59049]:
+        for world in [1, 2, 3, 8]:
+            r = [shard_range(npaths, k, world) for k in range(world)]
+            assert r[0][0] == 0 and r[-1][1] == npaths
+            assert all(r[k][1] == r[k + 1][0] for k in range(world - 1))
+            assert max(h - l for l, h in r) - min(h - l for l, h in r) <= 1
+
+
+def _gloo_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+
+    from hcgpu.parallel import shard_range
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    lo, hi = shard_range(1000, rank, world)
+    ms = torch.tensor([10.0 + rank])
+    dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+    cnt = torch.tensor([hi - lo])
+    dist.all_reduce(cnt)
+    out.put((rank, lo, hi, float(ms.item()), int(cnt.item())))
+    dist.destroy_process_group()
+
+
+def test_two_rank_sharding_gloo():
+    import multiprocessing as mp
+    import socket
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(120)
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert got[0][1:3] == (0, 500) and got[1][1:3] == (500, 1000)
+    assert all(g[3] == 11.0 and g[4] == 1000 for g in got)
