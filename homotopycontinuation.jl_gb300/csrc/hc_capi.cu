@@ -710,3 +710,182 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
 
 }  // extern "C"
 
+// =========================================================================================
+// hc_track_noalloc: a tracking call that performs no device memory allocation.
+//
+// Some callers cannot call cudaMalloc: code running under an allocator that owns all device
+// memory (a framework's caching pool, a memory-capped sandbox, an embedded runtime) or code
+// that must not allocate on its hot path. For them this entry point keeps the scratch memory
+// of the tracking kernel — the work-queue head, the counters, the cancel flag and the
+// compiled homotopy tables — in the file-scope array below instead of in handle-owned
+// allocations. The caller still passes the device buffers for start solutions, results and
+// endpoints.
+//
+// Limits and sharing rules:
+//   * the array holds HC_NOALLOC_SCRATCH_BYTES (1 MiB) on every GPU that loads this library,
+//     for the life of the process; homotopies whose compiled tables exceed
+//     HC_NOALLOC_MAX_PROGRAM_BYTES are rejected with HC_ERR_TOO_LARGE;
+//   * every call on a device uses the same array and leaves its contents behind; the queue
+//     head and counters are cleared at the start of each call, the tables are overwritten;
+//     calls whose kernels overlap on the GPU race on the array and must be serialised by the
+//     caller (for instance by issuing them on one stream);
+//   * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
+//     once for that device; make that first call outside any stream capture.
+// =========================================================================================
+namespace {
+
+constexpr size_t HC_NOALLOC_SCRATCH_BYTES = 1u << 20;
+constexpr size_t HC_NOALLOC_HEADER_BYTES = 256;  // queue head, 9 counters, cancel flag
+constexpr size_t HC_NOALLOC_MAX_PROGRAM_BYTES = HC_NOALLOC_SCRATCH_BYTES - HC_NOALLOC_HEADER_BYTES;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[HC_NOALLOC_SCRATCH_BYTES];
+
+constexpr int HC_NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[HC_NOALLOC_MAX_DEVICES] = {nullptr};
+
+// device address of g_noalloc_scratch on the current device (looked up once per device)
+cudaError_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= HC_NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = (unsigned char*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
+                                const double* G_coef, int nF, const int32_t* F_eq, const int32_t* F_exps,
+                                const double* F_coef, double gamma_re, double gamma_im, int64_t npaths,
+                                const double* d_starts, int endgame, double t1_re, double t1_im, double t0_re,
+                                double t0_im, hc_path_result* d_results, double* d_solutions, void* stream) {
+  hc_handle* h = nullptr;  // errors go to the library-wide message
+  if (!opts) return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: null options");
+  if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: need 1 <= n <= 32");
+  if (nG < 0 || nF < 0 || (nG > 0 && (!G_eq || !G_exps || !G_coef)) || (nF > 0 && (!F_eq || !F_exps || !F_coef)))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: bad term table");
+  if (!std::isfinite(gamma_re) || !std::isfinite(gamma_im))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: gamma must be finite");
+  if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: npaths < 0");
+  if (npaths == 0) return HC_OK;
+  if (!d_starts || !d_results || !d_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: null buffer");
+  if (opts->precision != HC_PREC_FP64 && opts->precision != HC_PREC_MIXED)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: unknown precision");
+  HostProg P;
+  std::string err;
+  int rc = build_program(n, nG, G_eq, G_exps, G_coef, nF, F_eq, F_exps, F_coef, P, err);
+  if (rc != HC_OK) return fail(h, rc, "hc_track_noalloc: " + err);
+  WarpLayout L = make_warp_layout(P);
+  TableLayout T = make_table_layout(P, opts->precision);
+  // compiled tables: packed exactly as hc_set_homotopy packs them
+  std::vector<char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    size_t o = (blob.size() + 15) & ~(size_t)15;
+    blob.resize(o + ((bytes + 15) & ~(size_t)15), 0);
+    if (bytes) memcpy(blob.data() + o, src, bytes);
+    return o;
+  };
+  size_t o_mdef = put(P.mdef.data(), P.mdef.size() * sizeof(int2));
+  size_t o_lev = put(P.lev.data(), P.lev.size() * sizeof(int));
+  size_t o_c64 = put(P.vcoef64.data(), P.vcoef64.size() * sizeof(double2));
+  size_t o_c32 = put(P.vcoef32.data(), P.vcoef32.size() * sizeof(float2));
+  size_t o_mono = put(P.vmono.data(), P.vmono.size() * sizeof(uint16_t));
+  size_t o_jcode = put(P.jcode.data(), P.jcode.size() * sizeof(uint32_t));
+  size_t off[2][3];
+  HostProg::Rows* rows[2] = {&P.val, &P.jac};
+  for (int q = 0; q < 2; ++q) {
+    off[q][0] = put(rows[q]->seg.data(), rows[q]->seg.size() * sizeof(int4));
+    off[q][1] = put(rows[q]->lane_seg.data(), rows[q]->lane_seg.size() * sizeof(int));
+    off[q][2] = put(rows[q]->row_slot.data(), rows[q]->row_slot.size() * sizeof(int));
+  }
+  if (blob.size() > HC_NOALLOC_MAX_PROGRAM_BYTES)
+    return fail(h, HC_ERR_TOO_LARGE,
+                "hc_track_noalloc: compiled homotopy needs " + std::to_string(blob.size()) +
+                    " bytes, the static scratch holds " + std::to_string(HC_NOALLOC_MAX_PROGRAM_BYTES));
+  unsigned char* scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: cudaGetSymbolAddress");
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: device query");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char* prog = scratch + HC_NOALLOC_HEADER_BYTES;
+  e = cudaMemsetAsync(scratch, 0, HC_NOALLOC_HEADER_BYTES, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: staging the tables");
+  DevProg D{};
+  D.n = n;
+  D.M = P.M;
+  D.nlev = P.nlev;
+  D.top = P.top;
+  D.mdef = (const int2*)(prog + o_mdef);
+  D.lev = (const int*)(prog + o_lev);
+  D.vcoef64 = (const double2*)(prog + o_c64);
+  D.vcoef32 = (const float2*)(prog + o_c32);
+  D.vmono = (const uint16_t*)(prog + o_mono);
+  D.jcode = (const uint32_t*)(prog + o_jcode);
+  DevRows* drows[2] = {&D.val, &D.jac};
+  for (int q = 0; q < 2; ++q) {
+    DevRows& X = *drows[q];
+    X.nrows = rows[q]->nrows;
+    X.nterms = q == 0 ? (int)P.vcoef64.size() : (int)P.jcode.size();
+    X.nslots = rows[q]->nslots;
+    X.nseg = (int)rows[q]->seg.size();
+    X.seg = (const int4*)(prog + off[q][0]);
+    X.lane_seg = (const int*)(prog + off[q][1]);
+    X.row_slot = (const int*)(prog + off[q][2]);
+  }
+  D.gamma_re = gamma_re;
+  D.gamma_im = gamma_im;
+  Launch la{};
+  la.P = D;
+  la.O = *opts;
+  la.L = L;
+  la.T = T;
+  la.npaths = npaths;
+  la.starts = (const double2*)d_starts;
+  la.res = d_results;
+  la.sol = (double2*)d_solutions;
+  la.val = nullptr;
+  la.last = nullptr;
+  la.mode = endgame ? 1 : 0;
+  la.t1_re = t1_re;
+  la.t1_im = t1_im;
+  la.t0_re = t0_re;
+  la.t0_im = t0_im;
+  la.counter = (unsigned long long*)scratch;
+  la.stats = (unsigned long long*)scratch + 1;
+  la.cancel = (volatile int*)(scratch + 128);
+  la.log = nullptr;
+  la.log_count = nullptr;
+  la.log_cap = 0;
+  const size_t smem_cap = 227 * 1024;
+  int wpc = opts->warps_per_cta;
+  if (wpc <= 0) wpc = std::max(1, (int)std::min<size_t>(8, (smem_cap - T.bytes) / L.bytes));
+  size_t smem = (size_t)T.bytes + (size_t)wpc * L.bytes;
+  while (wpc > 1 && smem > smem_cap) {
+    --wpc;
+    smem = (size_t)T.bytes + (size_t)wpc * L.bytes;
+  }
+  if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "hc_track_noalloc: working set exceeds shared memory");
+  int bps = 0;
+  e = occupancy(opts->precision, wpc, smem, &bps);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: occupancy");
+  if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_noalloc: kernel does not fit on an SM");
+  if (opts->ctas_per_sm > 0) bps = std::min(bps, opts->ctas_per_sm);
+  int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
+  int blocks = (int)std::min<int64_t>((int64_t)bps * sms, want);
+  e = launch_track(la, blocks, wpc, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: launch");
+  return HC_OK;
+}

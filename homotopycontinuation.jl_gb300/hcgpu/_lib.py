@@ -83,7 +83,7 @@ RESULT_DTYPE = np.dtype(
 EXPORTS = [
     "hc_default_options", "hc_create", "hc_destroy", "hc_set_options", "hc_set_homotopy",
     "hc_track", "hc_track_device", "hc_cancel", "hc_last_error", "hc_last_stats", "hc_fma_peak",
-    "hc_set_step_log", "hc_get_step_log",
+    "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc",
 ]
 STEP_LOG_FIELDS = 20
 
@@ -125,6 +125,9 @@ def load(build_if_missing: bool = True):
     L.hc_fma_peak.argtypes = [P, P]
     L.hc_set_step_log.argtypes = [P, ct.c_int64, ct.c_int64, ct.c_int64]
     L.hc_get_step_log.argtypes = [P, P, ct.c_int64, P]
+    L.hc_track_noalloc.argtypes = [ct.POINTER(Options), ct.c_int, ct.c_int, P, P, P, ct.c_int, P, P, P,
+                                   ct.c_double, ct.c_double, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double,
+                                   ct.c_double, ct.c_double, P, P, P]
     _lib = L
     return L
 

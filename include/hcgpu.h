@@ -144,6 +144,24 @@ int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t pat
  * of records the call produced (which may exceed the capacity). */
 int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_records);
 
+/* Track a batch without allocating any device memory. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc (code running under an allocator that owns all
+ * device memory, a memory-capped sandbox, or a hot path that must not allocate): options,
+ * homotopy term tables (host arrays, as for hc_set_homotopy) and device buffers for the start
+ * solutions, results and endpoints go in; the kernel's scratch (work-queue head, counters,
+ * cancel flag, compiled tables) lives in a 1 MiB static device array of the library instead
+ * of handle-owned allocations. Compiled tables above 1 MiB - 256 bytes are rejected with
+ * HC_ERR_TOO_LARGE. All calls on a device share that array: calls whose kernels overlap on
+ * the GPU race and must be serialised (e.g. one stream). The first call on a device looks up
+ * the array's address; make it outside any stream capture. Asynchronous on `stream`
+ * (a cudaStream_t, NULL = legacy default stream). */
+int hc_track_noalloc(const hc_options* opts, int n, int nG, const int32_t* G_eq,
+                     const int32_t* G_exps, const double* G_coef, int nF, const int32_t* F_eq,
+                     const int32_t* F_exps, const double* F_coef, double gamma_re,
+                     double gamma_im, int64_t npaths, const double* d_starts, int endgame,
+                     double t1_re, double t1_im, double t0_re, double t0_im,
+                     hc_path_result* d_results, double* d_solutions, void* stream);
+
 /* FP64 and FP32 CUDA-core FMA throughput of the current GPU in TFLOP/s, measured by a
  * short microbenchmark: the roofline denominators of this FP-pipe-bound path. No
  * counterpart in the reference. */
