@@ -41,6 +41,7 @@ def parse():
     p.add_argument("--step-control", default="plain", choices=["plain", "learned"])
     p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--paths", type=int, default=0, help="track only the first N paths (profiling cases)")
     return p.parse_args()
 
 
@@ -204,6 +205,8 @@ def main():
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     H, S = workload(args.seed + rank)
+    if args.paths:
+        S = S[: args.paths]
     npaths, n = S.shape
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)  # a real stream: the kernel and its events share it

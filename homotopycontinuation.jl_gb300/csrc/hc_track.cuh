@@ -1827,6 +1827,7 @@ struct PathTracker {
     for (int i = 0; i < n; ++i) {
       double toli = ait[i];
       if (toli < O->val_at_infinity_tol) {
+        if (MIXED && !j64) switch_to_fp64(ss.t());
         if (isnan(ais[i])) {
           bool allnan = __all_sync(FULL, LANE >= n || isnan(ais[LANE]));
           if (allnan) {
@@ -1906,6 +1907,7 @@ struct PathTracker {
     return err;
   }
   __device__ HC_NI void switch_to_singular() {  // :501-524
+    if (MIXED && !j64) switch_to_fp64(ss.t());
     singular_endgame = true;
     double t = ss.t().re;
     singular_start = t;
@@ -2020,6 +2022,10 @@ struct PathTracker {
     jtz1 = is_jump_to_zero;
     double t = ss.t().re;
     if (!(t <= O->endgame_start)) return ecode;
+    // mixed precision: in the endgame a path whose coordinates grow (‖x‖∞ > 1e4: FP32 loses
+    // range and accuracy on |x|^d) continues in FP64; so do paths flagged as diverging or
+    // entering the singular endgame (see check_at_infinity, switch_to_singular)
+    if (MIXED && !j64 && vnorm(ld(x), nullptr) > 1e4) switch_to_fp64(ss.t());
     if (steps_eg == 0) ext_steps_eg_start = ext_steps();
     steps_eg += 1;
     if (!step_success) return ecode;
