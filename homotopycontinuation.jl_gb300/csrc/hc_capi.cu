@@ -9,6 +9,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "hc_dev.h"
@@ -16,6 +17,8 @@
 namespace hcd {
 cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaStream_t stream);
 cudaError_t occupancy(int precision, int warps_per_cta, size_t smem, int* blocks_per_sm);
+cudaError_t prepare_batch(int precision, size_t smem, int warps_per_cta, int* blocks_per_sm);
+cudaError_t launch_batch(const BatchLaunch& bl, int blocks, int warps_per_cta, size_t smem, cudaStream_t stream);
 }  // namespace hcd
 
 using namespace hcd;
@@ -300,6 +303,64 @@ WarpLayout make_warp_layout(const HostProg& P) {
   return L;
 }
 
+// Device copy of a compiled program: every array 16-byte aligned and padded to 16 bytes,
+// appended to `blob`; bind_program turns the offsets into pointers once the blob is on the device.
+struct ProgOffsets {
+  size_t mdef, lev, c64, c32, mono, jcode, rows[2][3];
+};
+
+ProgOffsets pack_program(const HostProg& P, std::vector<char>& blob) {
+  auto put = [&](const void* src, size_t bytes) {
+    size_t o = (blob.size() + 15) & ~(size_t)15;
+    blob.resize(o + ((bytes + 15) & ~(size_t)15), 0);
+    if (bytes) memcpy(blob.data() + o, src, bytes);
+    return o;
+  };
+  ProgOffsets o;
+  o.mdef = put(P.mdef.data(), P.mdef.size() * sizeof(int2));
+  o.lev = put(P.lev.data(), P.lev.size() * sizeof(int));
+  o.c64 = put(P.vcoef64.data(), P.vcoef64.size() * sizeof(double2));
+  o.c32 = put(P.vcoef32.data(), P.vcoef32.size() * sizeof(float2));
+  o.mono = put(P.vmono.data(), P.vmono.size() * sizeof(uint16_t));
+  o.jcode = put(P.jcode.data(), P.jcode.size() * sizeof(uint32_t));
+  const HostProg::Rows* rows[2] = {&P.val, &P.jac};
+  for (int q = 0; q < 2; ++q) {
+    o.rows[q][0] = put(rows[q]->seg.data(), rows[q]->seg.size() * sizeof(int4));
+    o.rows[q][1] = put(rows[q]->lane_seg.data(), rows[q]->lane_seg.size() * sizeof(int));
+    o.rows[q][2] = put(rows[q]->row_slot.data(), rows[q]->row_slot.size() * sizeof(int));
+  }
+  return o;
+}
+
+DevProg bind_program(const HostProg& P, const ProgOffsets& o, const char* base, double gamma_re, double gamma_im) {
+  DevProg D{};
+  D.n = P.n;
+  D.M = P.M;
+  D.nlev = P.nlev;
+  D.top = P.top;
+  D.mdef = (const int2*)(base + o.mdef);
+  D.lev = (const int*)(base + o.lev);
+  D.vcoef64 = (const double2*)(base + o.c64);
+  D.vcoef32 = (const float2*)(base + o.c32);
+  D.vmono = (const uint16_t*)(base + o.mono);
+  D.jcode = (const uint32_t*)(base + o.jcode);
+  const HostProg::Rows* rows[2] = {&P.val, &P.jac};
+  DevRows* drows[2] = {&D.val, &D.jac};
+  for (int q = 0; q < 2; ++q) {
+    DevRows& X = *drows[q];
+    X.nrows = rows[q]->nrows;
+    X.nterms = q == 0 ? (int)P.vcoef64.size() : (int)P.jcode.size();
+    X.nslots = rows[q]->nslots;
+    X.nseg = (int)rows[q]->seg.size();
+    X.seg = (const int4*)(base + o.rows[q][0]);
+    X.lane_seg = (const int*)(base + o.rows[q][1]);
+    X.row_slot = (const int*)(base + o.rows[q][2]);
+  }
+  D.gamma_re = gamma_re;
+  D.gamma_im = gamma_im;
+  return D;
+}
+
 }  // namespace
 
 struct hc_handle {
@@ -320,11 +381,27 @@ struct hc_handle {
   double2* d_sol = nullptr;
   double* d_val = nullptr;
   double2* d_last = nullptr;
-  int64_t cap_paths = 0;
-  unsigned long long* d_counter = nullptr;  // [1 + 8 stats]
+  int64_t cap_paths = 0, cap_vec = 0;
+  unsigned long long* d_counter = nullptr;  // [queue head + HC_NSTATS counters]
   int* h_cancel = nullptr;                  // mapped host memory
   int* d_cancel = nullptr;
-  double stats[9] = {0};
+  double stats[HC_NSTATS] = {0};
+  StepModel* d_model = nullptr;  // learned step proposal (hc_set_step_model)
+  // batch of homotopies (hc_set_batch): programs, instance tables per precision, work units
+  bool has_batch = false;
+  char* d_bprog = nullptr;
+  size_t d_bprog_bytes = 0;
+  BatchInstance* d_binst[2] = {nullptr, nullptr};  // [precision]
+  BatchUnit* d_bunits = nullptr;
+  int bninst = 0, bnunits = 0;
+  int btbytes[2] = {0, 0}, bwstride = 0;
+  int64_t btotal_paths = 0, btotal_vec = 0;
+  // CUDA graph of the batch launch, re-recorded when its key changes
+  cudaGraphExec_t bgraph = nullptr;
+  const void* bgraph_key[3] = {nullptr, nullptr, nullptr};
+  int bgraph_endgame = -1, bgraph_blocks = 0, bgraph_wpc = 0;
+  unsigned long long bgraph_gen = 0;
+  unsigned long long generation = 1;  // bumped whenever options, model or batch change
   int last_blocks = 0, last_wpc = 0;
   cudaStream_t last_stream = nullptr;
   // step log
@@ -401,7 +478,7 @@ int hc_create(const hc_options* opts, hc_handle** out) {
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, 10 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, (1 + HC_NSTATS) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaHostAlloc(&h->h_cancel, sizeof(int), cudaHostAllocMapped);
   if (e == cudaSuccess) {
     *h->h_cancel = 0;
@@ -426,6 +503,12 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_val);
   cudaFree(h->d_last);
   cudaFree(h->d_counter);
+  cudaFree(h->d_model);
+  cudaFree(h->d_bprog);
+  cudaFree(h->d_binst[0]);
+  cudaFree(h->d_binst[1]);
+  cudaFree(h->d_bunits);
+  if (h->bgraph) cudaGraphExecDestroy(h->bgraph);
   cudaFree(h->d_log);
   cudaFree(h->d_log_count);
   if (h->h_cancel) cudaFreeHost(h->h_cancel);
@@ -437,7 +520,11 @@ int hc_set_options(hc_handle* h, const hc_options* opts) {
   if (!h || !opts) return fail(h, HC_ERR_INVALID_ARG, "hc_set_options: null pointer");
   if (opts->precision != HC_PREC_FP64 && opts->precision != HC_PREC_MIXED)
     return fail(h, HC_ERR_INVALID_ARG, "hc_set_options: unknown precision");
+  if (opts->step_control != HC_STEP_PLAIN && opts->step_control != HC_STEP_LEARNED &&
+      opts->step_control != HC_STEP_EXPLORE)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_options: unknown step control");
   h->opts = *opts;
+  ++h->generation;
   return HC_OK;
 }
 
@@ -458,28 +545,8 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   TableLayout T = make_table_layout(P, HC_PREC_MIXED);
   if ((size_t)T.bytes + L.bytes > 220 * 1024)
     return fail(h, HC_ERR_TOO_LARGE, "hc_set_homotopy: tables plus one path's working set exceed shared memory");
-  // pack device arrays (16-byte aligned, each padded to a multiple of 16 bytes)
   std::vector<char> blob;
-  auto put = [&](const void* src, size_t bytes) {
-    size_t o = (blob.size() + 15) & ~(size_t)15;
-    blob.resize(o + ((bytes + 15) & ~(size_t)15), 0);
-    if (bytes) memcpy(blob.data() + o, src, bytes);
-    return o;
-  };
-  size_t o_mdef = put(P.mdef.data(), P.mdef.size() * sizeof(int2));
-  size_t o_lev = put(P.lev.data(), P.lev.size() * sizeof(int));
-  size_t o_c64 = put(P.vcoef64.data(), P.vcoef64.size() * sizeof(double2));
-  size_t o_c32 = put(P.vcoef32.data(), P.vcoef32.size() * sizeof(float2));
-  size_t o_mono = put(P.vmono.data(), P.vmono.size() * sizeof(uint16_t));
-  size_t o_jcode = put(P.jcode.data(), P.jcode.size() * sizeof(uint32_t));
-  size_t off[2][3];
-  HostProg::Rows* rows[2] = {&P.val, &P.jac};
-  for (int q = 0; q < 2; ++q) {
-    HostProg::Rows& R = *rows[q];
-    off[q][0] = put(R.seg.data(), R.seg.size() * sizeof(int4));
-    off[q][1] = put(R.lane_seg.data(), R.lane_seg.size() * sizeof(int));
-    off[q][2] = put(R.row_slot.data(), R.row_slot.size() * sizeof(int));
-  }
+  ProgOffsets po = pack_program(P, blob);
   if (h->d_prog_bytes < blob.size()) {
     cudaFree(h->d_prog);
     h->d_prog = nullptr;
@@ -489,31 +556,7 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   }
   CK(cudaMemcpyAsync(h->d_prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  DevProg D{};
-  D.n = n;
-  D.M = P.M;
-  D.nlev = P.nlev;
-  D.top = P.top;
-  D.mdef = (const int2*)(h->d_prog + o_mdef);
-  D.lev = (const int*)(h->d_prog + o_lev);
-  D.vcoef64 = (const double2*)(h->d_prog + o_c64);
-  D.vcoef32 = (const float2*)(h->d_prog + o_c32);
-  D.vmono = (const uint16_t*)(h->d_prog + o_mono);
-  D.jcode = (const uint32_t*)(h->d_prog + o_jcode);
-  DevRows* drows[2] = {&D.val, &D.jac};
-  for (int q = 0; q < 2; ++q) {
-    HostProg::Rows& R = *rows[q];
-    DevRows& X = *drows[q];
-    X.nrows = R.nrows;
-    X.nterms = q == 0 ? (int)P.vcoef64.size() : (int)P.jcode.size();
-    X.nslots = R.nslots;
-    X.nseg = (int)R.seg.size();
-    X.seg = (const int4*)(h->d_prog + off[q][0]);
-    X.lane_seg = (const int*)(h->d_prog + off[q][1]);
-    X.row_slot = (const int*)(h->d_prog + off[q][2]);
-  }
-  D.gamma_re = gamma_re;
-  D.gamma_im = gamma_im;
+  DevProg D = bind_program(P, po, h->d_prog, gamma_re, gamma_im);
   h->prog = std::move(P);
   h->dprog = D;
   h->layout = L;
@@ -521,8 +564,9 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   return HC_OK;
 }
 
-static int ensure_capacity(hc_handle* h, int64_t npaths, int n) {
-  if (npaths <= h->cap_paths) return HC_OK;
+// handle-owned device buffers for `npaths` results and `nvec` complex vector elements
+static int ensure_capacity_v(hc_handle* h, int64_t npaths, int64_t nvec) {
+  if (npaths <= h->cap_paths && nvec <= h->cap_vec) return HC_OK;
   cudaFree(h->d_starts);
   cudaFree(h->d_res);
   cudaFree(h->d_sol);
@@ -533,16 +577,20 @@ static int ensure_capacity(hc_handle* h, int64_t npaths, int n) {
   h->d_sol = nullptr;
   h->d_val = nullptr;
   h->d_last = nullptr;
-  h->cap_paths = 0;
-  size_t nv = (size_t)npaths * n;
+  npaths = std::max(npaths, h->cap_paths);
+  nvec = std::max(nvec, h->cap_vec);
+  h->cap_paths = h->cap_vec = 0;
+  size_t nv = (size_t)nvec;
   CK(cudaMalloc(&h->d_starts, nv * sizeof(double2)));
   CK(cudaMalloc(&h->d_res, (size_t)npaths * sizeof(hc_path_result)));
   CK(cudaMalloc(&h->d_sol, nv * sizeof(double2)));
   CK(cudaMalloc(&h->d_val, nv * sizeof(double)));
   CK(cudaMalloc(&h->d_last, nv * sizeof(double2)));
   h->cap_paths = npaths;
+  h->cap_vec = nvec;
   return HC_OK;
 }
+static int ensure_capacity(hc_handle* h, int64_t npaths, int n) { return ensure_capacity_v(h, npaths, npaths * n); }
 
 int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
                     double t1_im, double t0_re, double t0_im, hc_path_result* d_results, double* d_solutions,
@@ -552,6 +600,8 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: npaths < 0");
   if (npaths == 0) return HC_OK;
   if (!d_starts || !d_results || !d_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null buffer");
+  if (h->opts.step_control == HC_STEP_LEARNED && !h->d_model)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: learned step control needs hc_set_step_model");
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
   Launch la{};
   la.P = h->dprog;
@@ -577,6 +627,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   la.log_cap = h->log_cap;
   la.log_lo = h->log_lo;
   la.log_hi = h->log_hi;
+  la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
   if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
   // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
   const size_t smem_cap = 227 * 1024;
@@ -596,7 +647,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
-  CK(cudaMemsetAsync(h->d_counter, 0, 10 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS) * sizeof(unsigned long long), s));
   CK(launch_track(la, blocks, wpc, s));
   h->last_blocks = blocks;
   h->last_wpc = wpc;
@@ -627,10 +678,10 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   if (out_valuation)
     CK(cudaMemcpyAsync(out_valuation, h->d_val, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (out_last) CK(cudaMemcpyAsync(out_last, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-  unsigned long long st[9];
-  CK(cudaMemcpyAsync(st, h->d_counter + 1, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long st[HC_NSTATS];
+  CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < 9; ++i) h->stats[i] = (double)st[i];
+  for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
   return HC_OK;
 }
@@ -668,6 +719,279 @@ int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_r
   return HC_OK;
 }
 
+static uint16_t to_bf16(float f) {  // round to nearest even; NaN stays NaN
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+int hc_set_step_model(hc_handle* h, const float* params, const float* mean, const float* std, double confidence,
+                      double max_factor) {
+  if (!h || !params || !mean || !std) return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: null pointer");
+  if (!(confidence > 0.0 && confidence < 1.0) || !(max_factor >= 1.0 && max_factor <= 1e3))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: need 0 < confidence < 1 and 1 <= max_factor <= 1000");
+  const int np = hc_mlp_num_params();
+  for (int i = 0; i < np; ++i)
+    if (!std::isfinite(params[i])) return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: non-finite parameter");
+  StepModel M;
+  std::memset(&M, 0, sizeof(M));
+  for (int i = 0; i < HC_NFEAT; ++i) {
+    if (!std::isfinite(mean[i]) || !(std[i] > 0.f) || !std::isfinite(std[i]))
+      return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: bad feature normalisation");
+    M.mean[i] = mean[i];
+    M.stdinv[i] = 1.0f / std[i];
+  }
+  M.c = (float)std::log(confidence / (1.0 - confidence));
+  M.logmax = (float)std::log(max_factor);
+  // parameter layout of hc_mlp.cu: W1[64][12] b1[64] W2[64][64] b2[64] W3[2][64] b3[2]
+  const float* p = params;
+  for (int i = 0; i < 64 * HC_NFEAT; ++i) M.W1[i] = to_bf16(*p++);
+  for (int i = 0; i < 64; ++i) M.b1[i] = *p++;
+  for (int i = 0; i < 64 * 64; ++i) M.W2[i] = to_bf16(*p++);
+  for (int i = 0; i < 64; ++i) M.b2[i] = *p++;
+  for (int i = 0; i < 2 * 64; ++i) M.W3[i] = to_bf16(*p++);
+  for (int i = 0; i < 2; ++i) M.b3[i] = *p++;
+  if (p - params != np) return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: parameter layout mismatch");
+  if (!h->d_model) CK(cudaMalloc(&h->d_model, sizeof(StepModel)));
+  CK(cudaMemcpyAsync(h->d_model, &M, sizeof(StepModel), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  ++h->generation;
+  return HC_OK;
+}
+
+// ---------------------------------------------------------------------------- batches
+int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, const int32_t* unit_paths,
+                 int64_t* total_paths, int64_t* total_elements) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: null handle");
+  if (ninstances < 1 || !inst) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: need at least one instance");
+  for (int i = 0; i < ninstances; ++i) {
+    const hc_instance_desc& d = inst[i];
+    std::string at = "hc_set_batch: instance " + std::to_string(i) + ": ";
+    if (d.n < 1 || d.n > 32) return fail(h, HC_ERR_UNSUPPORTED, at + "need 1 <= n <= 32");
+    if (d.nG < 0 || d.nF < 0 || (d.nG > 0 && (!d.G_eq || !d.G_exps || !d.G_coef)) ||
+        (d.nF > 0 && (!d.F_eq || !d.F_exps || !d.F_coef)))
+      return fail(h, HC_ERR_INVALID_ARG, at + "bad term table");
+    if (!std::isfinite(d.gamma_re) || !std::isfinite(d.gamma_im))
+      return fail(h, HC_ERR_INVALID_ARG, at + "gamma must be finite");
+    if (d.npaths < 0 || d.npaths > (int64_t)1 << 30) return fail(h, HC_ERR_INVALID_ARG, at + "bad npaths");
+  }
+  if (unit_paths)
+    for (int n = 0; n <= 32; ++n)
+      if (unit_paths[n] < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: negative unit_paths entry");
+  // compile the programs on all host cores
+  std::vector<HostProg> P(ninstances);
+  std::vector<int> rcs(ninstances, HC_OK);
+  std::vector<std::string> errs(ninstances);
+  {
+    int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    nt = std::min(nt, ninstances);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t] {
+        for (int i = t; i < ninstances; i += nt) {
+          const hc_instance_desc& d = inst[i];
+          rcs[i] = build_program(d.n, d.nG, d.G_eq, d.G_exps, d.G_coef, d.nF, d.F_eq, d.F_exps, d.F_coef, P[i],
+                                 errs[i]);
+        }
+      });
+    for (auto& x : th) x.join();
+  }
+  for (int i = 0; i < ninstances; ++i)
+    if (rcs[i] != HC_OK) return fail(h, rcs[i], "hc_set_batch: instance " + std::to_string(i) + ": " + errs[i]);
+  std::vector<char> blob;
+  std::vector<ProgOffsets> off(ninstances);
+  std::vector<BatchInstance> I[2];
+  I[0].resize(ninstances);
+  I[1].resize(ninstances);
+  int tb[2] = {0, 0}, ws = 0;
+  int64_t tp = 0, tv = 0;
+  for (int i = 0; i < ninstances; ++i) {
+    WarpLayout L = make_warp_layout(P[i]);
+    TableLayout T32 = make_table_layout(P[i], HC_PREC_MIXED);
+    if ((size_t)HC_LAUNCH_SMEM + T32.bytes + L.bytes > 220 * 1024)
+      return fail(h, HC_ERR_TOO_LARGE,
+                  "hc_set_batch: instance " + std::to_string(i) + ": tables plus one path exceed shared memory");
+    off[i] = pack_program(P[i], blob);
+    for (int q = 0; q < 2; ++q) {
+      BatchInstance& B = I[q][i];
+      B.T = make_table_layout(P[i], q == 0 ? HC_PREC_FP64 : HC_PREC_MIXED);
+      B.L = L;
+      B.npaths = inst[i].npaths;
+      B.path_off = tp;
+      B.vec_off = tv;
+      tb[q] = std::max(tb[q], B.T.bytes);
+    }
+    ws = std::max(ws, L.bytes);
+    tp += inst[i].npaths;
+    tv += inst[i].npaths * inst[i].n;
+  }
+  // work units, largest estimated cost first (monomial evaluations and the LU per path)
+  int wpc_est = (int)std::max<int64_t>(1, std::min<int64_t>(8, (227 * 1024 - HC_LAUNCH_SMEM - tb[1]) / ws));
+  struct U {
+    BatchUnit u;
+    double cost;
+  };
+  std::vector<U> units;
+  for (int i = 0; i < ninstances; ++i) {
+    int n = inst[i].n;
+    int64_t up = unit_paths && unit_paths[n] > 0 ? unit_paths[n] : 4 * wpc_est;
+    double per_path = (double)P[i].M * n + (double)n * n * n + (double)P[i].jcode.size();
+    for (int64_t lo = 0; lo < inst[i].npaths; lo += up) {
+      int64_t hi = std::min<int64_t>(inst[i].npaths, lo + up);
+      units.push_back({BatchUnit{i, (int)lo, (int)hi, 0}, per_path * (double)(hi - lo)});
+    }
+  }
+  std::stable_sort(units.begin(), units.end(), [](const U& a, const U& b) { return a.cost > b.cost; });
+  std::vector<BatchUnit> hu(units.size());
+  for (size_t k = 0; k < units.size(); ++k) hu[k] = units[k].u;
+  // upload: programs, instance tables (both precisions), units
+  h->has_batch = false;
+  if (h->d_bprog_bytes < blob.size()) {
+    cudaFree(h->d_bprog);
+    h->d_bprog = nullptr;
+    h->d_bprog_bytes = 0;
+    CK(cudaMalloc(&h->d_bprog, blob.size()));
+    h->d_bprog_bytes = blob.size();
+  }
+  for (int i = 0; i < ninstances; ++i) {
+    DevProg D = bind_program(P[i], off[i], h->d_bprog, inst[i].gamma_re, inst[i].gamma_im);
+    I[0][i].P = D;
+    I[1][i].P = D;
+  }
+  for (int q = 0; q < 2; ++q) {
+    cudaFree(h->d_binst[q]);
+    h->d_binst[q] = nullptr;
+    CK(cudaMalloc(&h->d_binst[q], (size_t)ninstances * sizeof(BatchInstance)));
+  }
+  cudaFree(h->d_bunits);
+  h->d_bunits = nullptr;
+  CK(cudaMalloc(&h->d_bunits, std::max<size_t>(1, hu.size()) * sizeof(BatchUnit)));
+  CK(cudaMemcpyAsync(h->d_bprog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
+  for (int q = 0; q < 2; ++q)
+    CK(cudaMemcpyAsync(h->d_binst[q], I[q].data(), (size_t)ninstances * sizeof(BatchInstance),
+                       cudaMemcpyHostToDevice, h->stream));
+  if (!hu.empty())
+    CK(cudaMemcpyAsync(h->d_bunits, hu.data(), hu.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->bninst = ninstances;
+  h->bnunits = (int)hu.size();
+  h->btbytes[0] = tb[0];
+  h->btbytes[1] = tb[1];
+  h->bwstride = ws;
+  h->btotal_paths = tp;
+  h->btotal_vec = tv;
+  h->has_batch = true;
+  ++h->generation;
+  if (total_paths) *total_paths = tp;
+  if (total_elements) *total_elements = tv;
+  return HC_OK;
+}
+
+int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_path_result* d_results,
+                          double* d_solutions, void* stream) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: null handle");
+  if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_batch_device: call hc_set_batch first");
+  if (h->btotal_paths == 0) return HC_OK;
+  if (!d_starts || !d_results || !d_solutions)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: null buffer");
+  if (h->opts.step_control == HC_STEP_LEARNED && !h->d_model)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: learned step control needs hc_set_step_model");
+  const int q = h->opts.precision == HC_PREC_MIXED ? 1 : 0;
+  const size_t smem_cap = 227 * 1024;
+  const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
+  int wpc = h->opts.warps_per_cta;
+  if (wpc <= 0) wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride));
+  size_t smem = fixed + (size_t)wpc * h->bwstride;
+  while (wpc > 1 && smem > smem_cap) {
+    --wpc;
+    smem = fixed + (size_t)wpc * h->bwstride;
+  }
+  if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "hc_track_batch_device: working set exceeds shared memory");
+  int bps = 0;
+  CK(prepare_batch(h->opts.precision, smem, wpc, &bps));
+  if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_batch_device: kernel does not fit on an SM");
+  if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
+  int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, h->bnunits);
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  const bool same = h->bgraph && h->bgraph_key[0] == d_starts && h->bgraph_key[1] == d_results &&
+                    h->bgraph_key[2] == d_solutions && h->bgraph_endgame == (endgame ? 1 : 0) &&
+                    h->bgraph_blocks == blocks && h->bgraph_wpc == wpc && h->bgraph_gen == h->generation;
+  if (!same) {
+    if (h->bgraph) cudaGraphExecDestroy(h->bgraph);
+    h->bgraph = nullptr;
+    BatchLaunch bl{};
+    Launch& la = bl.base;
+    la.O = h->opts;
+    la.npaths = h->btotal_paths;
+    la.starts = (const double2*)d_starts;
+    la.res = d_results;
+    la.sol = (double2*)d_solutions;
+    la.mode = endgame ? 1 : 0;
+    la.t1_re = 1.0;
+    la.t0_re = 0.0;
+    la.counter = h->d_counter;
+    la.cancel = h->d_cancel;
+    la.stats = h->d_counter + 1;
+    la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+    bl.inst = h->d_binst[q];
+    bl.units = h->d_bunits;
+    bl.nunits = h->bnunits;
+    bl.tbytes = h->btbytes[q];
+    bl.wstride = h->bwstride;
+    // record: clear the queue head and counters, then the kernel
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS) * sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) e = launch_batch(bl, blocks, wpc, smem, h->stream);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->bgraph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      h->bgraph = nullptr;
+      return cuda_fail(h, e, "hc_track_batch_device: recording the launch");
+    }
+    h->bgraph_key[0] = d_starts;
+    h->bgraph_key[1] = d_results;
+    h->bgraph_key[2] = d_solutions;
+    h->bgraph_endgame = endgame ? 1 : 0;
+    h->bgraph_blocks = blocks;
+    h->bgraph_wpc = wpc;
+    h->bgraph_gen = h->generation;
+  }
+  CK(cudaGraphLaunch(h->bgraph, s));
+  h->last_blocks = blocks;
+  h->last_wpc = wpc;
+  h->last_stream = s;
+  return HC_OK;
+}
+
+int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_result* out_results,
+                   double* out_solutions) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch: null handle");
+  if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_batch: call hc_set_batch first");
+  if (h->btotal_paths == 0) return HC_OK;
+  if (!starts || !out_results || !out_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch: null buffer");
+  int rc = ensure_capacity_v(h, h->btotal_paths, h->btotal_vec);
+  if (rc != HC_OK) return rc;
+  size_t nv = (size_t)h->btotal_vec;
+  *h->h_cancel = 0;
+  CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  rc = hc_track_batch_device(h, (const double*)h->d_starts, endgame, h->d_res, (double*)h->d_sol, nullptr);
+  if (rc != HC_OK) return rc;
+  CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)h->btotal_paths * sizeof(hc_path_result),
+                     cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long st[HC_NSTATS];
+  CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
+  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
+  return HC_OK;
+}
+
 int hc_cancel(hc_handle* h) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_cancel: null handle");
   __atomic_store_n(h->h_cancel, 1, __ATOMIC_SEQ_CST);
@@ -683,18 +1007,18 @@ const char* hc_last_error(hc_handle* h) {
 int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
   if (h->last_blocks > 0) {  // counters of the last call (hc_track or hc_track_device) on this handle
-    unsigned long long st[9];
-    CK(cudaMemcpyAsync(st, h->d_counter + 1, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->last_stream));
+    unsigned long long st[HC_NSTATS];
+    CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->last_stream));
     CK(cudaStreamSynchronize(h->last_stream));
-    for (int i = 0; i < 9; ++i) h->stats[i] = (double)st[i];
+    for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
   }
   // [0] paths, [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double
   // residuals, [4] Taylor orders (Σ K), [5] LU factorizations, [6] triangular solve pairs,
   // [7] FP32 Taylor evaluations redone in FP64, [8] paths moved to FP64 (mixed precision);
   // derived: [9] monomials M, [10] value terms, [11] Jacobian terms, [12] blocks, [13] warps
   // per block, [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree
-  // monomial offset
-  double all[17];
+  // monomial offset; [17] learned step proposals made, [18] of them rejected by Newton
+  double all[19];
   for (int i = 0; i < 9; ++i) all[i] = h->stats[i];
   all[9] = h->prog.M;
   all[10] = (double)h->prog.val_terms;
@@ -704,7 +1028,9 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   all[14] = h->layout.bytes;
   all[15] = make_table_layout(h->prog, h->opts.precision).bytes;
   all[16] = h->prog.top;
-  for (int i = 0; i < nout && i < 17; ++i) out[i] = all[i];
+  all[17] = h->stats[9];
+  all[18] = h->stats[10];
+  for (int i = 0; i < nout && i < 19; ++i) out[i] = all[i];
   return HC_OK;
 }
 
@@ -735,7 +1061,8 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
 namespace {
 
 constexpr size_t HC_NOALLOC_SCRATCH_BYTES = 1u << 20;
-constexpr size_t HC_NOALLOC_HEADER_BYTES = 256;  // queue head, 9 counters, cancel flag
+constexpr size_t HC_NOALLOC_HEADER_BYTES = 256;  // queue head, HC_NSTATS counters, cancel flag at +128
+static_assert((1 + HC_NSTATS) * sizeof(unsigned long long) <= 128, "counters overlap the cancel flag");
 constexpr size_t HC_NOALLOC_MAX_PROGRAM_BYTES = HC_NOALLOC_SCRATCH_BYTES - HC_NOALLOC_HEADER_BYTES;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[HC_NOALLOC_SCRATCH_BYTES];
@@ -770,6 +1097,8 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
                                 double t0_im, hc_path_result* d_results, double* d_solutions, void* stream) {
   hc_handle* h = nullptr;  // errors go to the library-wide message
   if (!opts) return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: null options");
+  if (opts->step_control == HC_STEP_LEARNED)
+    return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: learned step control needs a handle (hc_set_step_model)");
   if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: need 1 <= n <= 32");
   if (nG < 0 || nF < 0 || (nG > 0 && (!G_eq || !G_exps || !G_coef)) || (nF > 0 && (!F_eq || !F_exps || !F_coef)))
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: bad term table");
@@ -788,25 +1117,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   TableLayout T = make_table_layout(P, opts->precision);
   // compiled tables: packed exactly as hc_set_homotopy packs them
   std::vector<char> blob;
-  auto put = [&](const void* src, size_t bytes) {
-    size_t o = (blob.size() + 15) & ~(size_t)15;
-    blob.resize(o + ((bytes + 15) & ~(size_t)15), 0);
-    if (bytes) memcpy(blob.data() + o, src, bytes);
-    return o;
-  };
-  size_t o_mdef = put(P.mdef.data(), P.mdef.size() * sizeof(int2));
-  size_t o_lev = put(P.lev.data(), P.lev.size() * sizeof(int));
-  size_t o_c64 = put(P.vcoef64.data(), P.vcoef64.size() * sizeof(double2));
-  size_t o_c32 = put(P.vcoef32.data(), P.vcoef32.size() * sizeof(float2));
-  size_t o_mono = put(P.vmono.data(), P.vmono.size() * sizeof(uint16_t));
-  size_t o_jcode = put(P.jcode.data(), P.jcode.size() * sizeof(uint32_t));
-  size_t off[2][3];
-  HostProg::Rows* rows[2] = {&P.val, &P.jac};
-  for (int q = 0; q < 2; ++q) {
-    off[q][0] = put(rows[q]->seg.data(), rows[q]->seg.size() * sizeof(int4));
-    off[q][1] = put(rows[q]->lane_seg.data(), rows[q]->lane_seg.size() * sizeof(int));
-    off[q][2] = put(rows[q]->row_slot.data(), rows[q]->row_slot.size() * sizeof(int));
-  }
+  ProgOffsets po = pack_program(P, blob);
   if (blob.size() > HC_NOALLOC_MAX_PROGRAM_BYTES)
     return fail(h, HC_ERR_TOO_LARGE,
                 "hc_track_noalloc: compiled homotopy needs " + std::to_string(blob.size()) +
@@ -823,30 +1134,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   e = cudaMemsetAsync(scratch, 0, HC_NOALLOC_HEADER_BYTES, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: staging the tables");
-  DevProg D{};
-  D.n = n;
-  D.M = P.M;
-  D.nlev = P.nlev;
-  D.top = P.top;
-  D.mdef = (const int2*)(prog + o_mdef);
-  D.lev = (const int*)(prog + o_lev);
-  D.vcoef64 = (const double2*)(prog + o_c64);
-  D.vcoef32 = (const float2*)(prog + o_c32);
-  D.vmono = (const uint16_t*)(prog + o_mono);
-  D.jcode = (const uint32_t*)(prog + o_jcode);
-  DevRows* drows[2] = {&D.val, &D.jac};
-  for (int q = 0; q < 2; ++q) {
-    DevRows& X = *drows[q];
-    X.nrows = rows[q]->nrows;
-    X.nterms = q == 0 ? (int)P.vcoef64.size() : (int)P.jcode.size();
-    X.nslots = rows[q]->nslots;
-    X.nseg = (int)rows[q]->seg.size();
-    X.seg = (const int4*)(prog + off[q][0]);
-    X.lane_seg = (const int*)(prog + off[q][1]);
-    X.row_slot = (const int*)(prog + off[q][2]);
-  }
-  D.gamma_re = gamma_re;
-  D.gamma_im = gamma_im;
+  DevProg D = bind_program(P, po, (const char*)prog, gamma_re, gamma_im);
   Launch la{};
   la.P = D;
   la.O = *opts;
@@ -869,6 +1157,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   la.log = nullptr;
   la.log_count = nullptr;
   la.log_cap = 0;
+  la.model = nullptr;
   const size_t smem_cap = 227 * 1024;
   int wpc = opts->warps_per_cta;
   if (wpc <= 0) wpc = std::max(1, (int)std::min<size_t>(8, (smem_cap - T.bytes) / L.bytes));

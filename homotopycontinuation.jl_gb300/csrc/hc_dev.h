@@ -55,7 +55,25 @@ struct WarpLayout {
 };
 constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
 constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
-constexpr int HC_LOG_FIELDS = 20;  // doubles per step-log record
+constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
+constexpr int HC_NFEAT = 12;       // step features of the learned proposal
+constexpr int HC_NSTATS = 11;      // device counters of a tracking call
+
+// Step-proposal network as the tracker reads it: normalisation, BF16 weights, FP32 biases
+// (12→64→64→2; see hc_mlp.cu for the parameter layout and the loss).
+struct StepModel {
+  float mean[HC_NFEAT], stdinv[HC_NFEAT];
+  float c;       // logit of the target acceptance probability
+  float logmax;  // log of the largest step multiplier proposed
+  float pad[6];
+  uint16_t W1[64 * HC_NFEAT];
+  float b1[64];
+  uint16_t W2[64 * 64];
+  float b2[64];
+  uint16_t W3[2 * 64];
+  float b3[2];
+  float pad2[2];
+};
 
 struct Launch {
   DevProg P;
@@ -77,6 +95,31 @@ struct Launch {
   double* log;
   unsigned long long* log_count;
   long long log_cap, log_lo, log_hi;
+  const StepModel* model;  // learned step control (options.step_control == HC_STEP_LEARNED)
 };
+
+// A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).
+// Instance i has its own compiled program; its results start at path_off and its start and
+// solution vectors at vec_off (complex elements). The CTAs of the persistent kernel take work
+// units — (instance, path range) — from a device queue, stage that instance's tables in
+// shared memory, and their warps pull the unit's paths from a shared-memory counter.
+struct BatchInstance {
+  DevProg P;
+  TableLayout T;
+  WarpLayout L;
+  int64_t npaths, path_off, vec_off;
+};
+struct BatchUnit {
+  int inst, lo, hi, pad;
+};
+struct BatchLaunch {
+  Launch base;  // options, queue head (units), counters, cancel flag, t range, output bases
+  const BatchInstance* inst;
+  const BatchUnit* units;
+  int nunits;
+  int tbytes;   // shared bytes reserved for the tables (maximum over the instances)
+  int wstride;  // shared bytes per warp (maximum over the instances)
+};
+constexpr int HC_LAUNCH_SMEM = (int)((sizeof(Launch) + 127) & ~(size_t)127);
 
 }  // namespace hcd

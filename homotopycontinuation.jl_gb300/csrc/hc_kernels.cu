@@ -14,6 +14,22 @@ __device__ __forceinline__ void stage(char* dst, const void* src, int bytes) {
 }
 
 template <bool MIXED>
+__device__ __forceinline__ void add_stats(unsigned long long* st, const PathTracker<MIXED>* T,
+                                          unsigned long long npaths_done) {
+  atomicAdd(st + 0, npaths_done);
+  atomicAdd(st + 1, T->c_evalj);
+  atomicAdd(st + 2, T->c_eval);
+  atomicAdd(st + 3, T->c_evaldd);
+  atomicAdd(st + 4, T->c_taylor);
+  atomicAdd(st + 5, T->c_lu);
+  atomicAdd(st + 6, T->c_solve);
+  atomicAdd(st + 7, T->c_taylor64);
+  atomicAdd(st + 8, T->c_switch64);
+  atomicAdd(st + 9, T->c_learned);
+  atomicAdd(st + 10, T->c_learned_rej);
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Launch la) {
   static_assert(sizeof(PathTracker<MIXED>) <= HC_STATE_BYTES, "tracker state exceeds its shared-memory slot");
   extern __shared__ __align__(16) char smem[];
@@ -28,6 +44,7 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
   char* wbase = smem + TL.bytes + (size_t)wib * la.L.bytes;
   PathTracker<MIXED>* T = (PathTracker<MIXED>*)(wbase + la.L.state);
   T->init(&la, wbase, smem);
+  T->reset_counters();
   __syncwarp();
   const int lane = threadIdx.x & 31;
   unsigned long long npaths_done = 0;
@@ -50,17 +67,80 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
     ++npaths_done;
   }
   __syncwarp();
-  if (lane == 0 && la.stats) {
-    atomicAdd(la.stats + 0, npaths_done);
-    atomicAdd(la.stats + 1, T->c_evalj);
-    atomicAdd(la.stats + 2, T->c_eval);
-    atomicAdd(la.stats + 3, T->c_evaldd);
-    atomicAdd(la.stats + 4, T->c_taylor);
-    atomicAdd(la.stats + 5, T->c_lu);
-    atomicAdd(la.stats + 6, T->c_solve);
-    atomicAdd(la.stats + 7, T->c_taylor64);
-    atomicAdd(la.stats + 8, T->c_switch64);
+  if (lane == 0 && la.stats) add_stats(la.stats, T, npaths_done);
+}
+
+// Batch kernel: shared memory = [Launch of the current unit][tables][warp 0][warp 1]...
+// Per unit: thread 0 takes the next unit and writes its Launch, all threads stage the
+// instance's tables, warps track the unit's paths, and a barrier closes the unit before the
+// tables are overwritten. Paths are numbered within their instance (path_number = k + 1).
+template <bool MIXED>
+__global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant__ BatchLaunch bl) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int s_unit;
+  __shared__ unsigned s_next;
+  Launch* la = (Launch*)smem;
+  char* tbase = smem + HC_LAUNCH_SMEM;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  char* wbase = tbase + bl.tbytes + (size_t)wib * bl.wstride;
+  PathTracker<MIXED>* T = (PathTracker<MIXED>*)wbase;  // WarpLayout::state == 0 for every instance
+  T->reset_counters();
+  unsigned long long npaths_done = 0;
+  while (true) {
+    __syncthreads();  // the previous unit is closed
+    if (threadIdx.x == 0) {
+      int u = (int)atomicAdd(bl.base.counter, 1ULL);
+      s_unit = u;
+      s_next = 0;
+      if (u < bl.nunits) {
+        const BatchInstance& I = bl.inst[bl.units[u].inst];
+        *la = bl.base;
+        la->P = I.P;
+        la->T = I.T;
+        la->L = I.L;
+        la->npaths = I.npaths;
+        la->starts = bl.base.starts + I.vec_off;
+        la->res = bl.base.res + I.path_off;
+        la->sol = bl.base.sol + I.vec_off;
+        la->val = bl.base.val ? bl.base.val + I.vec_off : nullptr;
+        la->last = bl.base.last ? bl.base.last + I.vec_off : nullptr;
+      }
+    }
+    __syncthreads();
+    const int u = s_unit;
+    if (u >= bl.nunits) break;
+    const BatchUnit U = bl.units[u];
+    const TableLayout& TL = la->T;
+    stage(tbase + TL.vcoef64, la->P.vcoef64, TL.n64);
+    if (MIXED) stage(tbase + TL.vcoef32, la->P.vcoef32, TL.n32);
+    stage(tbase + TL.vmono, la->P.vmono, TL.nmono);
+    stage(tbase + TL.jcode, la->P.jcode, TL.njcode);
+    stage(tbase + TL.mdef, la->P.mdef, TL.nmdef);
+    __syncthreads();
+    T->init(la, wbase, tbase);
+    __syncwarp();
+    while (true) {
+      unsigned k = 0;
+      if (lane == 0) k = atomicAdd(&s_next, 1u);
+      k = __shfl_sync(FULL, k, 0);
+      const int64_t kk = (int64_t)U.lo + k;
+      if (kk >= U.hi) break;
+      if (T->cancelled()) {
+        if (lane == 0) {
+          hc_path_result R;
+          memset(&R, 0, sizeof(R));
+          R.path_number = kk + 1;
+          R.return_code = la->mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
+          la->res[kk] = R;
+        }
+        continue;
+      }
+      T->run(kk);
+      ++npaths_done;
+    }
   }
+  __syncwarp();
+  if (lane == 0 && bl.base.stats) add_stats(bl.base.stats, T, npaths_done);
 }
 
 // host-callable launchers
@@ -76,6 +156,31 @@ cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaSt
   size_t smem = (size_t)la.T.bytes + (size_t)warps_per_cta * la.L.bytes;
   if (la.O.precision == HC_PREC_MIXED) return launch_t<true>(la, blocks, warps_per_cta, smem, stream);
   return launch_t<false>(la, blocks, warps_per_cta, smem, stream);
+}
+
+cudaError_t prepare_batch(int precision, size_t smem, int warps_per_cta, int* blocks_per_sm) {
+  cudaError_t e;
+  if (precision == HC_PREC_MIXED) {
+    e = cudaFuncSetAttribute(track_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, track_batch_kernel<true>, 32 * warps_per_cta,
+                                                        smem);
+  } else {
+    e = cudaFuncSetAttribute(track_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, track_batch_kernel<false>,
+                                                        32 * warps_per_cta, smem);
+  }
+  return e;
+}
+
+// launch only (prepare_batch sets the shared-memory attribute first, outside stream capture)
+cudaError_t launch_batch(const BatchLaunch& bl, int blocks, int warps_per_cta, size_t smem, cudaStream_t stream) {
+  if (bl.base.O.precision == HC_PREC_MIXED)
+    track_batch_kernel<true><<<blocks, 32 * warps_per_cta, smem, stream>>>(bl);
+  else
+    track_batch_kernel<false><<<blocks, 32 * warps_per_cta, smem, stream>>>(bl);
+  return cudaGetLastError();
 }
 
 cudaError_t occupancy(int precision, int warps_per_cta, size_t smem, int* blocks_per_sm) {

@@ -205,8 +205,17 @@ struct PathTracker {
 
   long long cur_path;
 
+  // ---- learned / exploratory step proposals (options.step_control)
+  float phi[HC_NFEAT];   // features that decided the current step's size
+  bool phi_valid;
+  float step_logf;       // log multiplier applied to the current step (0: plain rule)
+  double ds_plain_cur;   // plain proposal of the current step
+  unsigned acc_hist;     // 1 = accepted, newest in bit 0
+  int cooldown;          // accepted steps to wait after a rejected learned proposal
+
   // ---- counters
-  unsigned long long c_evalj, c_eval, c_evaldd, c_taylor, c_lu, c_solve, c_taylor64, c_switch64;
+  unsigned long long c_evalj, c_eval, c_evaldd, c_taylor, c_lu, c_solve, c_taylor64, c_switch64, c_learned,
+      c_learned_rej;
 
   // all 32 lanes call init with the same arguments (the object is one per warp, in shared memory)
   __device__ void init(const Launch* la, char* base, char* tbase) {
@@ -273,7 +282,6 @@ struct PathTracker {
     factorized = scaled = false;
     Aprec = 64;
     j64 = false;
-    c_evalj = c_eval = c_evaldd = c_taylor = c_lu = c_solve = c_taylor64 = c_switch64 = 0;
     ca = O->a;
     ch_a = h_fn(ca);
     k_sq12ha = sqrt(1 - 2 * ch_a);
@@ -285,6 +293,11 @@ struct PathTracker {
     k_tolacc = pow(ca, (double)((1 << O->min_newton_iters) - 1)) * ch_a;
     k_a7h = pow(ca, 7.0) * ch_a;
     k_a5h = pow(ca, 5.0) * ch_a;
+  }
+
+  __device__ void reset_counters() {
+    c_evalj = c_eval = c_evaldd = c_taylor = c_lu = c_solve = c_taylor64 = c_switch64 = 0;
+    c_learned = c_learned_rej = 0;
   }
 
   // host cancel flag, read by lane 0 and broadcast so the warp stays converged
@@ -1475,6 +1488,11 @@ struct PathTracker {
 
   // init! (:639-754); returns is_tracking
   __device__ HC_NI bool tracker_init(c64 t1, c64 t0) {
+    phi_valid = false;
+    step_logf = 0.f;
+    ds_plain_cur = 0.0;
+    acc_hist = 0xffu;
+    cooldown = 0;
     j64 = false;
     omega_reseed = false;
     pred_delta = 0.0;
@@ -1605,9 +1623,125 @@ struct PathTracker {
     }
     norm_dx0 = res.norm_dx0;
     update_stepsize(res);
+    if (O->step_control != HC_STEP_PLAIN) propose_next(res, t, logging, pre);
+    else if (logging) log_step(t, pre, res);
     check_terminated();
-    if (logging) log_step(t, pre, res);
     return last_steps_failed == 0;
+  }
+
+  // ---- learned / exploratory step proposals ---------------------------------------------
+  // After a step, the plain rule (update_stepsize!, src/tracker.jl:541-588) has proposed Δs.
+  //   explore: the proposal of the next step is multiplied by f = 6^u, u uniform from a hash of
+  //            (path, step) — data for training;
+  //   learned: f = exp(network(features)) ∈ [1, exp(logmax)].
+  // A rejected enlarged proposal falls back to this step's plain proposal (then two accepted
+  // plain steps before the next learned proposal); Newton's contraction test judges every step.
+  // c_learned counts proposals the network enlarged, c_learned_rej those Newton rejected.
+  __device__ HC_NI void propose_next(const NewtonResult& res, c64 t_prev, bool logging, const double* pre) {
+    const bool accepted = last_steps_failed == 0;
+    acc_hist = (acc_hist << 1) | (accepted ? 1u : 0u);
+    if (!accepted && step_logf > 0.f) {
+      ss.propose(jmin(ds_plain_cur, ss.Ds()));
+      if (O->step_control == HC_STEP_LEARNED) {
+        ++c_learned_rej;
+        cooldown = 2;
+      }
+    }
+    if (logging) log_step(t_prev, pre, res);
+    float logf = 0.f;
+    bool valid = false;
+    double dsp = ss.Ds();
+    if (accepted && !ss.is_done()) {
+      compute_features(res, dsp);
+      valid = true;
+      if (O->step_control == HC_STEP_EXPLORE) {
+        unsigned long long z = (unsigned long long)cur_path * 0x9E3779B97F4A7C15ull + (unsigned long long)steps();
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        logf = (float)((double)(z >> 11) * 0x1p-53 * 1.791759469228055);  // ln 6
+      } else if (O->step_control == HC_STEP_LEARNED && a->model) {
+        if (cooldown > 0) {
+          --cooldown;
+        } else {
+          logf = mlp_logf();
+        }
+      }
+    }
+    if (logf > 0.f) {
+      // an enlarged step stays within 0.75 τ (β_τ of the reference's "fast" parameters,
+      // src/tracker.jl:58-62), never below the plain proposal; the applied multiplier is kept
+      double ds = jmin(dsp * exp((double)logf), jmax(dsp, 0.75 * tau));
+      ss.propose(ds);
+      logf = (float)log(ss.Ds() / dsp);
+      if (!(logf > 0.f)) {
+        logf = 0.f;
+        ss.propose(dsp);
+      } else if (O->step_control == HC_STEP_LEARNED) {
+        ++c_learned;
+      }
+    }
+    phi_valid = valid;
+    step_logf = logf;
+    ds_plain_cur = dsp;
+  }
+  // the 12 features of the step that was just accepted (all lanes hold the same values)
+  __device__ HC_NI void compute_features(const NewtonResult& res, double dsp) {
+    auto lg = [](double v) -> float {
+      double l = log10(v);
+      if (!(l == l)) return 0.f;
+      return (float)fmin(40.0, fmax(-40.0, l));
+    };
+    double xnorm = vnorm(ld(x), nullptr);
+    phi[0] = (float)ss.t().re;
+    phi[1] = lg(Ds_prev);
+    phi[2] = lg(tau);
+    phi[3] = lg(fmax(res.theta == res.theta ? res.theta : 1e-20, 1e-20));
+    phi[4] = lg(local_error);
+    phi[5] = lg(xnorm);
+    phi[6] = lg(omega);
+    phi[7] = lg(dsp / tau);
+    phi[8] = (float)__popc(acc_hist & 0xffu) * 0.125f;
+    phi[9] = (float)res.iters * 0.25f;
+    phi[10] = lg(mu);
+    phi[11] = lg(dsp);
+  }
+  // network inference: lane l computes hidden units l and l+32 (FP32 on BF16 weights)
+  __device__ HC_NI float mlp_logf() {
+    const StepModel* M = a->model;
+    float xin[HC_NFEAT];
+#pragma unroll
+    for (int i = 0; i < HC_NFEAT; ++i) xin[i] = (phi[i] - M->mean[i]) * M->stdinv[i];
+    auto bf = [](uint16_t v) { return __uint_as_float(((unsigned)v) << 16); };
+    const int u0 = LANE, u1 = LANE + 32;
+    float h0 = M->b1[u0], h1 = M->b1[u1];
+#pragma unroll
+    for (int i = 0; i < HC_NFEAT; ++i) {
+      h0 += bf(M->W1[u0 * HC_NFEAT + i]) * xin[i];
+      h1 += bf(M->W1[u1 * HC_NFEAT + i]) * xin[i];
+    }
+    h0 = fmaxf(h0, 0.f);
+    h1 = fmaxf(h1, 0.f);
+    float g0 = M->b2[u0], g1 = M->b2[u1];
+    for (int v = 0; v < 64; ++v) {
+      float hv = __shfl_sync(FULL, v < 32 ? h0 : h1, v & 31);
+      g0 += bf(M->W2[u0 * 64 + v]) * hv;
+      g1 += bf(M->W2[u1 * 64 + v]) * hv;
+    }
+    g0 = fmaxf(g0, 0.f);
+    g1 = fmaxf(g1, 0.f);
+    float p1 = bf(M->W3[u0]) * g0 + bf(M->W3[u1]) * g1;
+    float p2 = bf(M->W3[64 + u0]) * g0 + bf(M->W3[64 + u1]) * g1;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      p1 += __shfl_xor_sync(FULL, p1, o);
+      p2 += __shfl_xor_sync(FULL, p2, o);
+    }
+    float o1 = p1 + M->b3[0], o2 = p2 + M->b3[1];
+    float k = (o2 > 20.f ? o2 : log1pf(expf(o2))) + 0.05f;
+    float lf = o1 - M->c / k;
+    if (!(lf == lf)) return 0.f;
+    return fminf(fmaxf(lf, 0.f), M->logmax);
   }
   // one record per attempted step (HC_LOG_FIELDS doubles), see include/hcgpu.h
   __device__ HC_NI void log_step(c64 t, const double* pre, const NewtonResult& res) {
@@ -1616,6 +1750,22 @@ struct PathTracker {
     idx = __shfl_sync(FULL, idx, 0);
     if (idx >= (unsigned long long)a->log_cap) return;
     double* rec = a->log + idx * HC_LOG_FIELDS;
+    // fields 20..35: the features and multiplier that decided this step's size
+    if (LANE < 16) {
+      int f = 20 + LANE;
+      double w2;
+      if (LANE < HC_NFEAT)
+        w2 = phi_valid ? (double)phi[LANE] : 0.0;
+      else if (LANE == 12)
+        w2 = step_logf;
+      else if (LANE == 13)
+        w2 = ds_plain_cur;
+      else if (LANE == 14)
+        w2 = phi_valid ? 1.0 : 0.0;
+      else
+        w2 = (double)O->step_control;
+      rec[f] = w2;
+    }
     double v = 0.0;
     switch (LANE) {
       case 0: v = (double)(cur_path + 1); break;
@@ -1640,7 +1790,7 @@ struct PathTracker {
       case 19: v = (double)accepted_steps; break;
       default: break;
     }
-    if (LANE < HC_LOG_FIELDS) rec[LANE] = v;
+    if (LANE < 20) rec[LANE] = v;
   }
   // mixed precision: continue this path with an FP64 Jacobian, Taylor series and LU; the
   // predictor is recomputed at the accepted point and ω re-estimated by the next correction

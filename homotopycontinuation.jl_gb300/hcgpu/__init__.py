@@ -15,6 +15,7 @@ from .systems import (
     uneven_instances,
     variables,
 )
+from .batch import BatchTracker, autotune_unit_paths, solve_batch
 from .tracking import (
     ENDGAME_CODES,
     TRACKER_CODES,

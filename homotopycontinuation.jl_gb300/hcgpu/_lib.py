@@ -13,7 +13,7 @@ HC_OK = 0
 STATUS = {0: "HC_OK", 1: "HC_ERR_INVALID_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NO_SYSTEM",
           4: "HC_ERR_CANCELLED", 5: "HC_ERR_UNSUPPORTED", 6: "HC_ERR_TOO_LARGE"}
 PREC_FP64, PREC_MIXED = 0, 1
-STEP_PLAIN, STEP_LEARNED = 0, 1
+STEP_PLAIN, STEP_LEARNED, STEP_EXPLORE = 0, 1, 2
 
 
 class Options(ct.Structure):
@@ -83,9 +83,11 @@ RESULT_DTYPE = np.dtype(
 EXPORTS = [
     "hc_default_options", "hc_create", "hc_destroy", "hc_set_options", "hc_set_homotopy",
     "hc_track", "hc_track_device", "hc_cancel", "hc_last_error", "hc_last_stats", "hc_fma_peak",
-    "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc",
+    "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc", "hc_set_step_model",
+    "hc_mlp_num_params", "hc_mlp_forward", "hc_mlp_grad", "hc_mlp_adam",
+    "hc_set_batch", "hc_track_batch_device", "hc_track_batch",
 ]
-STEP_LOG_FIELDS = 20
+STEP_LOG_FIELDS = 36
 
 _lib = None
 
@@ -125,6 +127,14 @@ def load(build_if_missing: bool = True):
     L.hc_fma_peak.argtypes = [P, P]
     L.hc_set_step_log.argtypes = [P, ct.c_int64, ct.c_int64, ct.c_int64]
     L.hc_get_step_log.argtypes = [P, P, ct.c_int64, P]
+    L.hc_set_step_model.argtypes = [P, P, P, P, ct.c_double, ct.c_double]
+    L.hc_set_batch.argtypes = [P, ct.c_int, P, P, P, P]
+    L.hc_track_batch_device.argtypes = [P, P, ct.c_int, P, P, P]
+    L.hc_track_batch.argtypes = [P, P, ct.c_int, P, P]
+    L.hc_mlp_num_params.argtypes = []
+    L.hc_mlp_forward.argtypes = [P, ct.c_int, P, P, P]
+    L.hc_mlp_grad.argtypes = [P, P, P, ct.c_int, P, P, P, P]
+    L.hc_mlp_adam.argtypes = [P, P, P, P, ct.c_int, ct.c_float, ct.c_float, P]
     L.hc_track_noalloc.argtypes = [ct.POINTER(Options), ct.c_int, ct.c_int, P, P, P, ct.c_int, P, P, P,
                                    ct.c_double, ct.c_double, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double,
                                    ct.c_double, ct.c_double, P, P, P]

@@ -1,0 +1,165 @@
+"""Batches of independent total-degree homotopies tracked in one GPU launch.
+
+The reference solves independent systems one ``solve(F_i)`` at a time (src/solve.jl:447-526),
+each running its own ``threaded_solve`` loop over paths (src/solve.jl:628-709). Here all
+instances of a batch share one persistent launch (``hc_set_batch`` / ``hc_track_batch``): CTAs
+take work units (instance, path range) from a device queue, stage that instance's compiled
+tables in shared memory, and their warps track the unit's paths. The launch is recorded once
+in a CUDA graph and replayed.
+
+    B = BatchTracker([total_degree_homotopy(F, g) for F, g in instances])
+    results = B.solve()                   # list of Result, one per instance
+    results = solve_batch(instances)      # the same in one call
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import time
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .systems import TotalDegreeHomotopy, total_degree_homotopy, total_degree_start_solutions
+from .tracking import (EndgameOptions, Result, TrackerOptions, _Handle, _path_results, make_options)
+
+
+class InstanceDesc(ct.Structure):
+    """hc_instance_desc (include/hcgpu.h)."""
+
+    _fields_ = [("n", ct.c_int32), ("nG", ct.c_int32), ("nF", ct.c_int32), ("reserved", ct.c_int32),
+                ("G_eq", ct.c_void_p), ("G_exps", ct.c_void_p), ("G_coef", ct.c_void_p),
+                ("F_eq", ct.c_void_p), ("F_exps", ct.c_void_p), ("F_coef", ct.c_void_p),
+                ("gamma_re", ct.c_double), ("gamma_im", ct.c_double), ("npaths", ct.c_int64)]
+
+
+class BatchTracker:
+    """Endgame trackers of many homotopies behind one handle and one launch."""
+
+    def __init__(self, homotopies: Sequence[TotalDegreeHomotopy], tracker_options: Optional[TrackerOptions] = None,
+                 endgame_options: Optional[EndgameOptions] = None, npaths: Optional[Sequence[int]] = None,
+                 unit_paths: Optional[dict] = None):
+        self.homotopies = list(homotopies)
+        self.tracker_options = tracker_options or TrackerOptions()
+        self.options = endgame_options or EndgameOptions()
+        self._h = _Handle(make_options(self.tracker_options, self.options))
+        self._h.setup_step_control(self.tracker_options)
+        if npaths is None:
+            npaths = [int(np.prod(H.degrees)) for H in self.homotopies]
+        self.npaths = np.asarray(npaths, dtype=np.int64)
+        self.n = np.array([H.n for H in self.homotopies], dtype=np.int64)
+        self.path_off = np.concatenate([[0], np.cumsum(self.npaths)])
+        self.vec_off = np.concatenate([[0], np.cumsum(self.npaths * self.n)])
+        self.unit_paths = dict(unit_paths or {})
+        self._upload()
+
+    def _upload(self):
+        descs = (InstanceDesc * len(self.homotopies))()
+        keep = []
+        for i, H in enumerate(self.homotopies):
+            Ge, Gx, Gc = H.G.term_arrays()
+            Fe, Fx, Fc = H.F.term_arrays()
+            keep.append((Ge, Gx, Gc, Fe, Fx, Fc))
+            d = descs[i]
+            d.n, d.nG, d.nF = H.n, len(Ge), len(Fe)
+            d.G_eq, d.G_exps, d.G_coef = Ge.ctypes.data, Gx.ctypes.data, Gc.ctypes.data
+            d.F_eq, d.F_exps, d.F_coef = Fe.ctypes.data, Fx.ctypes.data, Fc.ctypes.data
+            d.gamma_re, d.gamma_im = H.gamma.real, H.gamma.imag
+            d.npaths = int(self.npaths[i])
+        up = np.zeros(33, dtype=np.int32)
+        for n, u in self.unit_paths.items():
+            up[int(n)] = int(u)
+        tp = np.zeros(1, dtype=np.int64)
+        tv = np.zeros(1, dtype=np.int64)
+        P = _lib.ptr
+        rc = self._h.L.hc_set_batch(self._h.h, len(self.homotopies), descs, P(up), P(tp), P(tv))
+        _lib.check(rc, self._h.h)
+        assert int(tp[0]) == int(self.path_off[-1]) and int(tv[0]) == int(self.vec_off[-1])
+        self.total_paths, self.total_elements = int(tp[0]), int(tv[0])
+
+    def set_unit_paths(self, unit_paths: dict):
+        self.unit_paths = dict(unit_paths)
+        self._upload()
+
+    def start_solutions(self):
+        """Concatenated total-degree start solutions of every instance (src/total_degree.jl:240-262)."""
+        out = np.empty(self.total_elements, dtype=np.complex128)
+        for i, H in enumerate(self.homotopies):
+            S = total_degree_start_solutions(H.degrees, np.arange(self.npaths[i]))
+            out[self.vec_off[i]:self.vec_off[i + 1]] = S.reshape(-1)
+        return out
+
+    def track_arrays(self, starts=None):
+        """Raw results (RESULT_DTYPE, all instances) and concatenated endpoints."""
+        if starts is None:
+            starts = self.start_solutions()
+        starts = np.ascontiguousarray(np.asarray(starts, dtype=np.complex128).reshape(-1))
+        if starts.shape[0] != self.total_elements:
+            raise ValueError(f"expected {self.total_elements} start values, got {starts.shape[0]}")
+        res = np.zeros(self.total_paths, dtype=_lib.RESULT_DTYPE)
+        sol = np.zeros(self.total_elements, dtype=np.complex128)
+        P = _lib.ptr
+        _lib.check(self._h.L.hc_track_batch(self._h.h, P(starts), 1, P(res), P(sol)), self._h.h)
+        return res, sol
+
+    def split(self, res, sol):
+        """Per-instance (results, endpoints[npaths, n]) views."""
+        return [(res[self.path_off[i]:self.path_off[i + 1]],
+                 sol[self.vec_off[i]:self.vec_off[i + 1]].reshape(-1, int(self.n[i])))
+                for i in range(len(self.homotopies))]
+
+    def solve(self, starts=None, seed=None):
+        res, sol = self.track_arrays(starts)
+        out = []
+        for i, (r, x) in enumerate(self.split(res, sol)):
+            n = int(self.n[i])
+            zv = np.zeros((r.shape[0], n))
+            zl = np.zeros((r.shape[0], n), dtype=np.complex128)
+            prs = _path_results(r, x, zv, zl, None, self.options.endgame_start)
+            out.append(Result(prs, seed=seed, start_system="total_degree"))
+        return out
+
+    def stats(self):
+        return self._h.stats()
+
+    def cancel(self):
+        self._h.cancel()
+
+
+def solve_batch(instances, tracker_options=None, endgame_options=None, unit_paths=None):
+    """Solve many independent square systems by total-degree homotopies in one launch.
+    ``instances``: (System, γ) pairs (as returned by systems.uneven_instances)."""
+    Hs = [total_degree_homotopy(F, g) for F, g in instances]
+    return BatchTracker(Hs, tracker_options, endgame_options, unit_paths=unit_paths).solve()
+
+
+def autotune_unit_paths(homotopies, tracker_options=None, candidates=(8, 16, 32, 64, 128), sample=None,
+                        repeats=1, verbose=False):
+    """Choose the paths per CTA work unit for every n in the batch: for each n, the batch of
+    that n's instances (or ``sample`` of them) is tracked with each candidate unit size and the
+    fastest is kept. Returns {n: unit_paths}."""
+    import torch
+
+    by_n = {}
+    for H in homotopies:
+        by_n.setdefault(H.n, []).append(H)
+    best = {}
+    for n, Hs in sorted(by_n.items()):
+        if sample:
+            Hs = Hs[:sample]
+        B = BatchTracker(Hs, tracker_options)
+        S = B.start_solutions()
+        times = {}
+        for c in candidates:
+            B.set_unit_paths({n: c})
+            B.track_arrays(S)  # records the graph
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(repeats):
+                B.track_arrays(S)
+            times[c] = (time.perf_counter() - t0) / repeats
+        best[n] = min(times, key=times.get)
+        if verbose:
+            print(f"autotune n={n}: {len(Hs)} instances, {B.total_paths} paths:",
+                  {c: round(t * 1e3, 2) for c, t in times.items()}, "ms ->", best[n], flush=True)
+    return best

@@ -54,7 +54,8 @@ class TrackerOptions:
     parameters: str = "default"
     # GPU knobs (no reference counterpart)
     precision: str = "fp64"  # "fp64" | "mixed"
-    step_control: str = "plain"  # "plain" | "learned"
+    step_control: str = "plain"  # "plain" | "learned" | "explore"
+    step_model: Optional[object] = None  # learn.StepModel for "learned"; None: the shipped model
     warps_per_cta: int = 0
     ctas_per_sm: int = 0
 
@@ -97,7 +98,8 @@ def make_options(tracker_options: Optional[TrackerOptions] = None,
         setattr(o, k, v)
     o.strict_beta_tau = min(0.75 * o.beta_tau, 0.4)
     o.precision = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[to.precision]
-    o.step_control = {"plain": _lib.STEP_PLAIN, "learned": _lib.STEP_LEARNED}[to.step_control]
+    o.step_control = {"plain": _lib.STEP_PLAIN, "learned": _lib.STEP_LEARNED,
+                      "explore": _lib.STEP_EXPLORE}[to.step_control]
     for f in fields(EndgameOptions):
         v = getattr(eo, f.name)
         setattr(o, f.name, int(v) if isinstance(v, bool) else v)
@@ -232,12 +234,26 @@ class _Handle:
 
     STAT_NAMES = ["paths", "evals_jac", "evals", "evals_dd", "taylor_orders", "lu", "solves", "taylor_fp64_redo",
                   "paths_to_fp64", "monomials", "value_terms", "jacobian_terms", "blocks", "warps_per_block",
-                  "smem_per_warp", "smem_tables", "top"]
+                  "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"]
 
     def stats(self):
-        out = np.zeros(17)
-        _lib.check(self.L.hc_last_stats(self.h, _lib.ptr(out), 17), self.h)
+        out = np.zeros(len(self.STAT_NAMES))
+        _lib.check(self.L.hc_last_stats(self.h, _lib.ptr(out), len(out)), self.h)
         return dict(zip(self.STAT_NAMES, out.tolist()))
+
+    def set_step_model(self, model):
+        """Load a learn.StepModel (network parameters and feature normalisation)."""
+        P = _lib.ptr
+        params = np.ascontiguousarray(model.params, dtype=np.float32)
+        mean = np.ascontiguousarray(model.mean, dtype=np.float32)
+        std = np.ascontiguousarray(model.std, dtype=np.float32)
+        _lib.check(self.L.hc_set_step_model(self.h, P(params), P(mean), P(std), float(model.confidence),
+                                            float(model.max_factor)), self.h)
+
+    def setup_step_control(self, to):
+        if to.step_control == "learned":
+            from . import learn
+            self.set_step_model(to.step_model if to.step_model is not None else learn.default_model())
 
     def cancel(self):
         self.L.hc_cancel(self.h)
@@ -290,6 +306,7 @@ class EndgameTracker:
         self.tracker_options = tracker_options or TrackerOptions()
         self.options = endgame_options or EndgameOptions()
         self._h = _Handle(make_options(self.tracker_options, self.options))
+        self._h.setup_step_control(self.tracker_options)
         self._h.set_homotopy(H)
 
     def track_arrays(self, starts, t1: float = 1.0):
@@ -318,6 +335,7 @@ class Tracker:
         self.homotopy = H
         self.options = options or TrackerOptions()
         self._h = _Handle(make_options(self.options, None))
+        self._h.setup_step_control(self.options)
         self._h.set_homotopy(H)
 
     def track_arrays(self, starts, t1=1.0, t0=0.0):

@@ -43,9 +43,11 @@ enum hc_status {
 enum hc_precision { HC_PREC_FP64 = 0, HC_PREC_MIXED = 1 };
 
 /* Step-size control. HC_STEP_PLAIN is update_stepsize! (src/tracker.jl:541-588).
- * HC_STEP_LEARNED lets a loaded MLP propose the step length after each accepted step; any
- * proposal the Newton contraction test rejects falls back to the plain rule. */
-enum hc_step_control { HC_STEP_PLAIN = 0, HC_STEP_LEARNED = 1 };
+ * HC_STEP_LEARNED lets the loaded network (hc_set_step_model) enlarge the plain proposal after
+ * each accepted step; a proposal the Newton contraction test rejects falls back to the plain
+ * one. HC_STEP_EXPLORE multiplies the plain proposal by a pseudo-random factor in [1, 6] and
+ * is used with the step log to collect training data. */
+enum hc_step_control { HC_STEP_PLAIN = 0, HC_STEP_LEARNED = 1, HC_STEP_EXPLORE = 2 };
 
 /* Mirrors TrackerOptions + TrackerParameters (src/tracker.jl:45-140) and EndgameOptions
  * (src/endgame_tracker.jl:47-72); hc_default_options fills in the reference defaults. */
@@ -130,15 +132,34 @@ const char* hc_last_error(hc_handle* h);
  * and the algorithmic FP64/FP32 flop counts used for the roofline (out[0..7]). */
 int hc_last_stats(hc_handle* h, double* out, int nout);
 
+/* Load the step-proposal network used with HC_STEP_LEARNED: `params` are the FP32 parameters
+ * (hc_mlp_num_params() floats, layout in hc_mlp.cu; stored as BF16 weights), `mean`/`std`
+ * normalise the 12 features, proposals target acceptance probability `confidence` and are
+ * capped at `max_factor` times the plain proposal. No counterpart in the reference. */
+int hc_set_step_model(hc_handle* h, const float* params, const float* mean, const float* std,
+                      double confidence, double max_factor);
+
+/* Step-proposal network kernels (BF16 tensor-core operands, FP32 accumulation), device
+ * pointers: forward out[B×2] = net(X[B×12]); mean BCE loss and gradient of logged steps
+ * (X, tried log-multipliers L, accepted flags Y); one Adam step. No reference counterpart. */
+int hc_mlp_num_params(void);
+int hc_mlp_forward(const float* d_X, int B, const float* d_params, float* d_out, void* stream);
+int hc_mlp_grad(const float* d_X, const float* d_L, const float* d_Y, int B, const float* d_params,
+                float* d_grad, float* d_loss, void* stream);
+int hc_mlp_adam(float* d_params, float* d_m, float* d_v, const float* d_grad, int step, float lr,
+                float weight_decay, void* stream);
+
 /* Step log: after this call, every step attempted on a path whose 0-based index lies in
  * [path_lo, path_hi) appends one record of HC_STEP_LOG_FIELDS doubles to a device buffer of
  * `capacity` records (capacity 0 disables logging). The fields follow the reference's
  * PathInfo trace (src/path_info.jl:3-21): path number, t (re, im), Δs tried, trust region,
  * local error, ω, μ (before the step), accepted, Newton iterations, θ, ‖Δx₀‖, ‖x‖∞,
  * previous Δs, next Δs, flags (extended precision | FP64-fallback << 1 | Newton code << 2),
- * ω and accuracy returned by the corrector, trust region after the step, accepted steps.
+ * ω and accuracy returned by the corrector, trust region after the step, accepted steps;
+ * then the 12 step features that decided this step's size, the log-multiplier applied, the
+ * plain proposal, a features-valid flag and the step-control mode (fields 20..35).
  * It is the training data of the learned step proposal. */
-#define HC_STEP_LOG_FIELDS 20
+#define HC_STEP_LOG_FIELDS 36
 int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t path_hi);
 /* Copy up to max_records records of the last call to `out`; *n_records receives the number
  * of records the call produced (which may exceed the capacity). */
@@ -161,6 +182,41 @@ int hc_track_noalloc(const hc_options* opts, int n, int nG, const int32_t* G_eq,
                      double gamma_im, int64_t npaths, const double* d_starts, int endgame,
                      double t1_re, double t1_im, double t0_re, double t0_im,
                      hc_path_result* d_results, double* d_solutions, void* stream);
+
+/* ---- Batches of independent homotopies (one launch) ----------------------------------
+ * Replaces one solve(F_i) per instance (src/solve.jl:447-526, each running threaded_solve,
+ * src/solve.jl:628-709) by a single persistent launch over all instances' paths. An instance
+ * is a straight-line homotopy given exactly as to hc_set_homotopy, plus its number of start
+ * solutions. Results are stored instance after instance (instance i's first result at
+ * Σ_{j<i} npaths_j, its first start/solution element at Σ_{j<i} npaths_j·n_j complex values);
+ * path_number counts within the instance (1-based), as in the per-instance solve. */
+typedef struct hc_instance_desc {
+  int32_t n, nG, nF, reserved;
+  const int32_t* G_eq;
+  const int32_t* G_exps;
+  const double* G_coef;
+  const int32_t* F_eq;
+  const int32_t* F_exps;
+  const double* F_coef;
+  double gamma_re, gamma_im;
+  int64_t npaths;
+} hc_instance_desc;
+
+/* Compile and upload a batch (replacing any previous batch of the handle). The kernel's CTAs
+ * take work units of at most unit_paths[n] paths of one instance with n variables
+ * (unit_paths: 33 entries indexed by n, NULL or 0 = 4 paths per warp of a CTA); units are
+ * queued largest estimated cost first. `total_paths` and `total_elements` (optional) receive
+ * Σ npaths_i and Σ npaths_i·n_i. */
+int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* instances,
+                 const int32_t* unit_paths, int64_t* total_paths, int64_t* total_elements);
+/* Track every path of the batch from t=1 to t=0 (endgame != 0: EndgameTracker) on device
+ * buffers; asynchronous on `stream` (NULL = the handle's stream). The launch is recorded in a
+ * CUDA graph the first time a set of buffers is used and replayed afterwards. */
+int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame,
+                          hc_path_result* d_results, double* d_solutions, void* stream);
+/* Same with host arrays; blocks until the results are in `out_results`/`out_solutions`. */
+int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_result* out_results,
+                   double* out_solutions);
 
 /* FP64 and FP32 CUDA-core FMA throughput of the current GPU in TFLOP/s, measured by a
  * short microbenchmark: the roofline denominators of this FP-pipe-bound path. No

@@ -1,0 +1,108 @@
+"""GPU tests of batched tracking (hc_set_batch / hc_track_batch): many independent
+homotopies of uneven size in one launch.
+
+Every path of a batch runs the same per-path code as a single-homotopy launch, so its result
+must equal, bit for bit, the one hc_track returns for its instance alone — whatever the work
+unit sizes and however often the recorded graph is replayed. Small instances are also checked
+against the CPU oracle."""
+import numpy as np
+import pytest
+
+import hcgpu as hc
+from _parity import REL_TOL, counts, oracle_track, rel_err
+from hcgpu import _lib
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["return_code", "t_re", "accuracy", "residual", "cond", "winding_number", "singular", "accepted_steps",
+          "rejected_steps", "steps_eg", "path_number"]
+
+
+def _batch(count, seed, max_n=8):
+    inst = [(F, g) for F, g in hc.uneven_instances(count, seed) if F.n <= max_n]
+    return [hc.total_degree_homotopy(F, g) for F, g in inst]
+
+
+def _same(ra, xa, rb, xb):
+    for f in FIELDS:
+        a, b = ra[f], rb[f]
+        assert np.array_equal(a, b, equal_nan=np.issubdtype(a.dtype, np.floating)), f
+    assert np.array_equal(xa, xb)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_equals_single_launches(precision):
+    Hs = _batch(24, seed=11, max_n=6)
+    to = hc.TrackerOptions(precision=precision)
+    B = hc.BatchTracker(Hs, to)
+    res, sol = B.track_arrays()
+    assert res.shape[0] == B.total_paths == sum(int(np.prod(H.degrees)) for H in Hs)
+    for i, (r, x) in enumerate(B.split(res, sol)):
+        T = hc.EndgameTracker(Hs[i], hc.TrackerOptions(precision=precision))
+        S = hc.total_degree_start_solutions(Hs[i].degrees)
+        r1, x1, _, _ = T.track_arrays(S)
+        _same(r, x, r1, x1)
+        assert list(r["path_number"]) == list(range(1, r.shape[0] + 1))
+    assert B.stats()["paths"] == B.total_paths
+
+
+def test_unit_size_and_graph_replay_do_not_change_results():
+    Hs = _batch(30, seed=12, max_n=7)
+    B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed"))
+    S = B.start_solutions()
+    r0, x0 = B.track_arrays(S)
+    r1, x1 = B.track_arrays(S)  # replay of the recorded graph
+    _same(r0, x0, r1, x1)
+    for up in ({n: 1 for n in range(3, 9)}, {n: 7 for n in range(3, 9)}, {3: 200, 5: 3, 8: 1000}):
+        B.set_unit_paths(up)
+        r2, x2 = B.track_arrays(S)
+        _same(r0, x0, r2, x2)
+
+
+def test_batch_against_oracle_small_instances():
+    """Instances with n ≤ 4: counts equal to the oracle's and nonsingular endpoints within 1e-10."""
+    Hs = _batch(40, seed=13, max_n=4)[:12]
+    B = hc.BatchTracker(Hs)
+    res, sol = B.track_arrays()
+    for i, (r, x) in enumerate(B.split(res, sol)):
+        S = hc.total_degree_start_solutions(Hs[i].degrees)
+        ro, xo, _, _ = oracle_track(Hs[i], S)
+        assert counts(r) == counts(ro)
+        both = (ro["return_code"] == 1) & (ro["singular"] == 0) & (r["return_code"] == 1) & (r["singular"] == 0)
+        if both.any():
+            assert rel_err(x[both], xo[both]).max() <= REL_TOL
+
+
+def test_solve_batch_results():
+    inst = [(F, g) for F, g in hc.uneven_instances(10, 14) if F.n <= 5]
+    results = hc.solve_batch(inst)
+    assert len(results) == len(inst)
+    for (F, g), R in zip(inst, results):
+        assert len(R) == int(np.prod(F.degrees()))
+        R1 = hc.solve(F, gamma=g)
+        assert hc.nnonsingular(R) == hc.nnonsingular(R1)
+        assert hc.nat_infinity(R) == hc.nat_infinity(R1)
+
+
+def test_batch_learned_step_control():
+    """The batch path honours the learned step control (same per-path code)."""
+    from hcgpu import learn
+
+    Hs = _batch(12, seed=15, max_n=6)
+    to = hc.TrackerOptions(precision="mixed", step_control="learned", step_model=learn.default_model())
+    B = hc.BatchTracker(Hs, to)
+    res, sol = B.track_arrays()
+    for i, (r, x) in enumerate(B.split(res, sol)):
+        T = hc.EndgameTracker(Hs[i], to)
+        r1, x1, _, _ = T.track_arrays(hc.total_degree_start_solutions(Hs[i].degrees))
+        _same(r, x, r1, x1)
+    assert B.stats()["learned_proposals"] > 0
+
+
+def test_batch_rejects_bad_input():
+    H = _batch(4, seed=16)[0]
+    with pytest.raises(_lib.HCError, match="npaths"):
+        hc.BatchTracker([H], npaths=[-1])
+    B = hc.BatchTracker([H])
+    with pytest.raises(ValueError):
+        B.track_arrays(np.zeros(3, dtype=np.complex128))

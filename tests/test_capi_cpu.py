@@ -48,6 +48,23 @@ def test_struct_layout_matches_header(tmp_path):
     assert ol == _lib.RESULT_DTYPE.fields["last_t"][1]
 
 
+def test_instance_desc_layout_matches_header(tmp_path):
+    from hcgpu.batch import InstanceDesc
+
+    src = tmp_path / "inst.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "hcgpu.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu\\n\", sizeof(hc_instance_desc), offsetof(hc_instance_desc, G_eq),"
+        " offsetof(hc_instance_desc, gamma_re), offsetof(hc_instance_desc, npaths));return 0;}\n")
+    exe = tmp_path / "inst"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    size, og, ogr, onp = map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split())
+    assert size == ct.sizeof(InstanceDesc)
+    assert og == InstanceDesc.G_eq.offset
+    assert ogr == InstanceDesc.gamma_re.offset
+    assert onp == InstanceDesc.npaths.offset
+
+
 def test_default_options_mirror_reference():
     o = _lib.default_options()
     # src/tracker.jl:45-62, :105-140 and src/endgame_tracker.jl:47-72
