@@ -38,7 +38,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    p.add_argument("--step-control", default="plain", choices=["plain", "learned"])
+    p.add_argument("--step-control", default="learned", choices=["plain", "learned"])
     p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--paths", type=int, default=0, help="track only the first N paths (profiling cases)")
@@ -342,7 +342,10 @@ def main():
             "max_rel_endpoint_err_vs_oracle_sample": rel_oracle,
             "codes_identical_to_oracle_sample": codes_equal,
             "device_counters": {k: stats[k] for k in ["evals_jac", "evals", "evals_dd", "taylor_orders", "lu",
-                                                     "solves", "taylor_fp64_redo", "paths_to_fp64"]},
+                                                     "solves", "taylor_fp64_redo", "paths_to_fp64",
+                                                     "learned_proposals", "learned_rejected"]},
+            "steps_per_path": float((res["accepted_steps"] + res["rejected_steps"]).mean()),
+            "steps_per_path_plain_fp64": float((res64["accepted_steps"] + res64["rejected_steps"]).mean()),
         }
         print(json.dumps(line), flush=True)
     if dist:

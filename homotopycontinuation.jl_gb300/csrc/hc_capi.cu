@@ -747,9 +747,11 @@ int hc_set_step_model(hc_handle* h, const float* params, const float* mean, cons
   M.logmax = (float)std::log(max_factor);
   // parameter layout of hc_mlp.cu: W1[64][12] b1[64] W2[64][64] b2[64] W3[2][64] b3[2]
   const float* p = params;
-  for (int i = 0; i < 64 * HC_NFEAT; ++i) M.W1[i] = to_bf16(*p++);
+  for (int u = 0; u < 64; ++u)
+    for (int i = 0; i < HC_NFEAT; ++i) M.W1T[i * 64 + u] = to_bf16(*p++);
   for (int i = 0; i < 64; ++i) M.b1[i] = *p++;
-  for (int i = 0; i < 64 * 64; ++i) M.W2[i] = to_bf16(*p++);
+  for (int u = 0; u < 64; ++u)
+    for (int v = 0; v < 64; ++v) M.W2T[v * 64 + u] = to_bf16(*p++);
   for (int i = 0; i < 64; ++i) M.b2[i] = *p++;
   for (int i = 0; i < 2 * 64; ++i) M.W3[i] = to_bf16(*p++);
   for (int i = 0; i < 2; ++i) M.b3[i] = *p++;

@@ -66,9 +66,9 @@ struct StepModel {
   float c;       // logit of the target acceptance probability
   float logmax;  // log of the largest step multiplier proposed
   float pad[6];
-  uint16_t W1[64 * HC_NFEAT];
+  uint16_t W1T[HC_NFEAT * 64];  // input-major: W1T[i*64 + u] = W1[u][i], so a warp reads 64 B
   float b1[64];
-  uint16_t W2[64 * 64];
+  uint16_t W2T[64 * 64];  // W2T[v*64 + u] = W2[u][v]
   float b2[64];
   uint16_t W3[2 * 64];
   float b3[2];

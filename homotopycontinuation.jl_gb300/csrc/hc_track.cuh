@@ -1581,10 +1581,12 @@ struct PathTracker {
     }
     if (MIXED && !j64) {
       res = newton<c32>(xb, xh, tp, mu, omega, extended_prec, false, accepted_steps == 0);
-      if (res.code != NEWT_CONVERGED) {
+      if (res.code != NEWT_CONVERGED && step_logf <= 0.f) {
         // The FP32 Jacobian could not carry the correction: switch the path to FP64, redo the
         // predictor at the accepted point (its FP32 coefficients may be the culprit) and
-        // retry this step with the same step size.
+        // retry this step with the same step size. A step enlarged beyond the plain proposal
+        // (learned / explore step control) that fails is rejected instead: the step size, not
+        // FP32, is the suspect, and the next attempt falls back to the plain proposal.
         switch_to_fp64(t);
         predict(t, Dt);
         res = newton<c64>(xb, xh, tp, mu, omega, extended_prec, false, accepted_steps == 0);
@@ -1717,16 +1719,16 @@ struct PathTracker {
     float h0 = M->b1[u0], h1 = M->b1[u1];
 #pragma unroll
     for (int i = 0; i < HC_NFEAT; ++i) {
-      h0 += bf(M->W1[u0 * HC_NFEAT + i]) * xin[i];
-      h1 += bf(M->W1[u1 * HC_NFEAT + i]) * xin[i];
+      h0 += bf(M->W1T[i * 64 + u0]) * xin[i];
+      h1 += bf(M->W1T[i * 64 + u1]) * xin[i];
     }
     h0 = fmaxf(h0, 0.f);
     h1 = fmaxf(h1, 0.f);
     float g0 = M->b2[u0], g1 = M->b2[u1];
     for (int v = 0; v < 64; ++v) {
       float hv = __shfl_sync(FULL, v < 32 ? h0 : h1, v & 31);
-      g0 += bf(M->W2[u0 * 64 + v]) * hv;
-      g1 += bf(M->W2[u1 * 64 + v]) * hv;
+      g0 += bf(M->W2T[v * 64 + u0]) * hv;
+      g1 += bf(M->W2T[v * 64 + u1]) * hv;
     }
     g0 = fmaxf(g0, 0.f);
     g1 = fmaxf(g1, 0.f);

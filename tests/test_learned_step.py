@@ -164,3 +164,33 @@ def test_learned_step_gain_held_out():
         steps_m = int(rm["accepted_steps"].sum() + rm["rejected_steps"].sum())
         assert stl["learned_proposals"] > 0
         assert steps_l <= 0.9 * steps_m, (steps_l, steps_m)
+
+
+def test_tracker_inference_matches_oracle():
+    """The multiplier the tracker applies after an accepted step (step-log field 32) equals the
+    oracle network on the logged features (fields 20..31, BF16-rounded weights), capped at
+    0.75 τ / Δs_plain as the tracker caps it."""
+    model = learn.default_model()
+    H, S = _family(2002, 64)
+    to = hc.TrackerOptions(precision="mixed", step_control="learned", step_model=model)
+    T = hc.EndgameTracker(H, to)
+    T._h.set_step_log(64 * 400, 0, 64)
+    T.track_arrays(S)
+    log = T._h.get_step_log()
+    rec = log[(log[:, 34] == 1.0) & (log[:, 32] > 0)]
+    assert rec.shape[0] > 64 * 10
+    phi = rec[:, 20:32]
+    pb = M.to_bf16(model.params)
+    # biases stay FP32 on the device; only weights are BF16
+    P = M.unpack(model.params.astype(np.float64))
+    Q = M.unpack(pb)
+    for b in ("b1", "b2", "b3"):
+        Q[b] = P[b]
+    net = M.propose_logf(M.pack(Q), model.mean.astype(np.float64), model.std.astype(np.float64), phi,
+                         model.confidence, model.max_factor)
+    cap = np.maximum(0.0, np.log(0.75) - np.log(10.0) * phi[:, 7])
+    expect = np.minimum(net, cap)
+    # the step is also clamped at the end of its segment (not logged), which only shortens it
+    assert (rec[:, 32] <= expect + 1e-3).all()
+    ok = np.abs(rec[:, 32] - expect) <= 1e-3
+    assert ok.mean() >= 0.97, (ok.mean(), rec[~ok][:5, 32], expect[~ok][:5])
