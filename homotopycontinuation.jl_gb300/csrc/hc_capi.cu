@@ -385,7 +385,7 @@ struct hc_handle {
   unsigned long long* d_counter = nullptr;  // [queue head + HC_NSTATS counters]
   int* h_cancel = nullptr;                  // mapped host memory
   int* d_cancel = nullptr;
-  double stats[HC_NSTATS] = {0};
+  double stats[HC_NSTATS + HC_NPHASE] = {0};
   StepModel* d_model = nullptr;  // learned step proposal (hc_set_step_model)
   // batch of homotopies (hc_set_batch): programs, instance tables per precision, work units
   bool has_batch = false;
@@ -478,7 +478,7 @@ int hc_create(const hc_options* opts, hc_handle** out) {
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, (1 + HC_NSTATS) * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_counter, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaHostAlloc(&h->h_cancel, sizeof(int), cudaHostAllocMapped);
   if (e == cudaSuccess) {
     *h->h_cancel = 0;
@@ -628,6 +628,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   la.log_lo = h->log_lo;
   la.log_hi = h->log_hi;
   la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+  la.phase = h->d_counter + 1 + HC_NSTATS;
   if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
   // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
   const size_t smem_cap = 227 * 1024;
@@ -647,7 +648,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
-  CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS) * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), s));
   CK(launch_track(la, blocks, wpc, s));
   h->last_blocks = blocks;
   h->last_wpc = wpc;
@@ -678,10 +679,10 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   if (out_valuation)
     CK(cudaMemcpyAsync(out_valuation, h->d_val, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (out_last) CK(cudaMemcpyAsync(out_last, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-  unsigned long long st[HC_NSTATS];
+  unsigned long long st[HC_NSTATS + HC_NPHASE];
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
+  for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
   return HC_OK;
 }
@@ -937,6 +938,7 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
     la.cancel = h->d_cancel;
     la.stats = h->d_counter + 1;
     la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+    la.phase = h->d_counter + 1 + HC_NSTATS;
     bl.inst = h->d_binst[q];
     bl.units = h->d_bunits;
     bl.nunits = h->bnunits;
@@ -945,7 +947,8 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
     // record: clear the queue head and counters, then the kernel
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS) * sizeof(unsigned long long), h->stream);
+    cudaError_t e =
+        cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), h->stream);
     if (e == cudaSuccess) e = launch_batch(bl, blocks, wpc, smem, h->stream);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e == cudaSuccess) e = e2;
@@ -986,10 +989,10 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
   CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)h->btotal_paths * sizeof(hc_path_result),
                      cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-  unsigned long long st[HC_NSTATS];
+  unsigned long long st[HC_NSTATS + HC_NPHASE];
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
+  for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
   return HC_OK;
 }
@@ -1009,18 +1012,19 @@ const char* hc_last_error(hc_handle* h) {
 int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
   if (h->last_blocks > 0) {  // counters of the last call (hc_track or hc_track_device) on this handle
-    unsigned long long st[HC_NSTATS];
+    unsigned long long st[HC_NSTATS + HC_NPHASE];
     CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->last_stream));
     CK(cudaStreamSynchronize(h->last_stream));
-    for (int i = 0; i < HC_NSTATS; ++i) h->stats[i] = (double)st[i];
+    for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   }
   // [0] paths, [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double
   // residuals, [4] Taylor orders (Σ K), [5] LU factorizations, [6] triangular solve pairs,
   // [7] FP32 Taylor evaluations redone in FP64, [8] paths moved to FP64 (mixed precision);
   // derived: [9] monomials M, [10] value terms, [11] Jacobian terms, [12] blocks, [13] warps
   // per block, [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree
-  // monomial offset; [17] learned step proposals made, [18] of them rejected by Newton
-  double all[19];
+  // monomial offset; [17] learned step proposals made, [18] of them rejected by Newton;
+  // [19 ..] cycle counters of the tracker phases (HcPhase order; profiling builds only)
+  double all[19 + HC_NPHASE];
   for (int i = 0; i < 9; ++i) all[i] = h->stats[i];
   all[9] = h->prog.M;
   all[10] = (double)h->prog.val_terms;
@@ -1032,7 +1036,8 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   all[16] = h->prog.top;
   all[17] = h->stats[9];
   all[18] = h->stats[10];
-  for (int i = 0; i < nout && i < 19; ++i) out[i] = all[i];
+  for (int k = 0; k < HC_NPHASE; ++k) all[19 + k] = h->stats[HC_NSTATS + k];
+  for (int i = 0; i < nout && i < 19 + HC_NPHASE; ++i) out[i] = all[i];
   return HC_OK;
 }
 
@@ -1160,6 +1165,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   la.log_count = nullptr;
   la.log_cap = 0;
   la.model = nullptr;
+  la.phase = nullptr;
   const size_t smem_cap = 227 * 1024;
   int wpc = opts->warps_per_cta;
   if (wpc <= 0) wpc = std::max(1, (int)std::min<size_t>(8, (smem_cap - T.bytes) / L.bytes));

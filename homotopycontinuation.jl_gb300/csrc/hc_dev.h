@@ -58,6 +58,14 @@ constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
 constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
 constexpr int HC_NFEAT = 12;       // step features of the learned proposal
 constexpr int HC_NSTATS = 11;      // device counters of a tracking call
+// Cycle counters of the tracker's phases, accumulated per warp (lane 0, clock64) in builds
+// compiled with -DHC_PHASE_CLOCKS and reported by hc_last_stats; zero otherwise. Phases nest
+// (a solve includes the factorization it triggers), so the counts are inclusive.
+enum HcPhase {
+  PH_RUN, PH_STEP, PH_PREDICTOR, PH_PREDICT, PH_NEWTON, PH_EVALJ, PH_EVAL, PH_TAYLOR, PH_LU, PH_SOLVE,
+  PH_NORM, PH_STEPSIZE, PH_ENDGAME, PH_MONO, PH_VALROWS, PH_JACROWS, PH_REFINE, PH_INIT, PH_COND, PH_DD,
+  HC_NPHASE
+};
 
 // Step-proposal network as the tracker reads it: normalisation, BF16 weights, FP32 biases
 // (12→64→64→2; see hc_mlp.cu for the parameter layout and the loss).
@@ -96,6 +104,7 @@ struct Launch {
   unsigned long long* log_count;
   long long log_cap, log_lo, log_hi;
   const StepModel* model;  // learned step control (options.step_control == HC_STEP_LEARNED)
+  unsigned long long* phase;  // [HC_NPHASE] phase cycle counters (profiling builds), may be null
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

@@ -28,6 +28,13 @@ __device__ __forceinline__ void add_stats(unsigned long long* st, const PathTrac
   atomicAdd(st + 9, T->c_learned);
   atomicAdd(st + 10, T->c_learned_rej);
 }
+template <bool MIXED>
+__device__ __forceinline__ void add_phases(unsigned long long* ph, const PathTracker<MIXED>* T) {
+#ifdef HC_PHASE_CLOCKS
+  if (ph)
+    for (int k = 0; k < HC_NPHASE; ++k) atomicAdd(ph + k, T->ph[k]);
+#endif
+}
 
 template <bool MIXED>
 __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Launch la) {
@@ -68,6 +75,7 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
   }
   __syncwarp();
   if (lane == 0 && la.stats) add_stats(la.stats, T, npaths_done);
+  if (lane == 0) add_phases(la.phase, T);
 }
 
 // Batch kernel: shared memory = [Launch of the current unit][tables][warp 0][warp 1]...
@@ -141,6 +149,7 @@ __global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant_
   }
   __syncwarp();
   if (lane == 0 && bl.base.stats) add_stats(bl.base.stats, T, npaths_done);
+  if (lane == 0) add_phases(bl.base.phase, T);
 }
 
 // host-callable launchers

@@ -132,6 +132,25 @@ __device__ __forceinline__ c64 cpow_int(c64 a, int k) {
 }
 
 // ------------------------------------------------------------------------------------------
+#ifdef HC_PHASE_CLOCKS
+// profiling builds: adds the cycles of the enclosing scope to one phase counter (lane 0)
+struct PhaseClock {
+  unsigned long long* acc;
+  long long t0;
+#ifdef __CUDA_ARCH__
+  __device__ explicit PhaseClock(unsigned long long* a) : acc(a), t0(clock64()) {}
+  __device__ ~PhaseClock() {
+    if ((threadIdx.x & 31) == 0) *acc += (unsigned long long)(clock64() - t0);
+  }
+#else
+  __device__ explicit PhaseClock(unsigned long long* a) : acc(a), t0(0) {}
+#endif
+};
+#define HC_PHASE(k) PhaseClock hc_phase_clock_(&ph[k])
+#else
+#define HC_PHASE(k)
+#endif
+
 template <bool MIXED>
 struct PathTracker {
   using JT = typename std::conditional<MIXED, c32, c64>::type;
@@ -216,6 +235,9 @@ struct PathTracker {
   // ---- counters
   unsigned long long c_evalj, c_eval, c_evaldd, c_taylor, c_lu, c_solve, c_taylor64, c_switch64, c_learned,
       c_learned_rej;
+#ifdef HC_PHASE_CLOCKS
+  mutable unsigned long long ph[HC_NPHASE];
+#endif
 
   // all 32 lanes call init with the same arguments (the object is one per warp, in shared memory)
   __device__ void init(const Launch* la, char* base, char* tbase) {
@@ -298,6 +320,9 @@ struct PathTracker {
   __device__ void reset_counters() {
     c_evalj = c_eval = c_evaldd = c_taylor = c_lu = c_solve = c_taylor64 = c_switch64 = 0;
     c_learned = c_learned_rej = 0;
+#ifdef HC_PHASE_CLOCKS
+    for (int k = 0; k < HC_NPHASE; ++k) ph[k] = 0;
+#endif
   }
 
   // host cancel flag, read by lane 0 and broadcast so the warp stays converged
@@ -318,6 +343,7 @@ struct PathTracker {
   // ‖x‖ with weights w (w == nullptr: InfNorm), x given per LANE
   // (the weights are applied as reciprocals, kept in winv next to w)
   __device__ HC_NI double vnorm(c64 xi, const double* wv) const {
+    HC_PHASE(PH_NORM);
     double d = 0.0;
     c64 q = xi;
     if (LANE < n && wv) q = xi * winv[LANE];
@@ -367,6 +393,7 @@ struct PathTracker {
   // ---------------------------------------------------------------- evaluation
   // monomial values (level by level; m = mono[parent] * x[var])
   __device__ HC_NI void eval_mono64(const c64* xv) {
+    HC_PHASE(PH_MONO);
     __syncwarp();
     if (LANE == 0) mono64[0] = C64(1.0);
     for (int L = 1; L < P->nlev; ++L) {
@@ -394,6 +421,7 @@ struct PathTracker {
   }
   // value rows on FP64 monomials: lane i < n returns F_i, G_i
   __device__ HC_NI void val_rows64(c64& Fi, c64& Gi) {
+    HC_PHASE(PH_VALROWS);
     const DevRows& R = P->val;
     c64* pp = (c64*)part;
     int s0 = __ldg(R.lane_seg + LANE), s1e = __ldg(R.lane_seg + LANE + 1);
@@ -424,6 +452,7 @@ struct PathTracker {
   // is (segment multiplier) × (value-term coefficient).
   template <class T>
   __device__ HC_NI void jac_rows(c64 ts64, c64 tt64) {
+    HC_PHASE(PH_JACROWS);
     const DevRows& R = P->jac;
     T* pp = (T*)part;
     const T* mv;
@@ -471,6 +500,7 @@ struct PathTracker {
 
   // H(x,t) (src/homotopies/straight_line_homotopy.jl:96-104) → out (vector)
   __device__ HC_NI void H_eval(const c64* xv, c64 t, c64* out) {
+    HC_PHASE(PH_EVAL);
     eval_mono64(xv);
     c64 F, G;
     val_rows64(F, G);
@@ -481,6 +511,7 @@ struct PathTracker {
   // H and its Jacobian (:106-124) in arithmetic T for the Jacobian
   template <class T>
   __device__ HC_NI void H_eval_jac(const c64* xv, c64 t) {
+    HC_PHASE(PH_EVALJ);
     eval_mono64(xv);
     if constexpr (std::is_same<T, c32>::value) mono_to32();
     c64 F, G;
@@ -495,6 +526,7 @@ struct PathTracker {
   }
   // double-double residual (:81-94), rounded to FP64 on store
   __device__ HC_NI void H_eval_dd(const c64* xv, c64 t, c64* out) {
+    HC_PHASE(PH_DD);
     __syncwarp();
     cdd* md = (cdd*)mono64;
     if (LANE == 0) md[0] = cdd_of(C64(1.0));
@@ -536,6 +568,7 @@ struct PathTracker {
   // (2^-21 · Σ|terms|) exceeds 1e-3 · |u_i| for some i: the caller then recomputes in FP64.
   template <class T>
   __device__ HC_NI bool H_taylor(int K, c64 t, c64* out) {
+    HC_PHASE(PH_TAYLOR);
     constexpr bool F32 = std::is_same<T, c32>::value;
     __syncwarp();
     T* S = (T*)mono64;
@@ -753,6 +786,7 @@ struct PathTracker {
     }
   }
   __device__ HC_NI void factorize() {
+    HC_PHASE(PH_LU);
     if (Aprec == 64)
       lu_factor_T<c64>();
     else
@@ -858,6 +892,7 @@ struct PathTracker {
   }
   // ldiv!(x, J, b[, norm]) (:833-862)
   __device__ HC_NI c64 jac_ldiv(c64 b, const double* wv) {
+    HC_PHASE(PH_SOLVE);
     if (wv && !factorized) {
       skeel_row_scaling(rs, wv, -30.0);
       apply_row_scaling();
@@ -880,6 +915,7 @@ struct PathTracker {
   }
   // fixed_precision_iterative_refinement! (:553-567)
   __device__ HC_NI double fp_refine_step(c64& xl, c64 b, const double* wv) {
+    HC_PHASE(PH_REFINE);
     __syncwarp();
     c64 acc = C64(0.0);
     for (int j = 0; j < n; ++j) {
@@ -980,6 +1016,7 @@ struct PathTracker {
   // cond of the current Jacobian (:745-774). FP64 decisions: an FP32 Jacobian is first
   // re-evaluated in FP64 at the point where it was last evaluated.
   __device__ HC_NI double ws_cond(const double* dl, const double* dr) {
+    HC_PHASE(PH_COND);
     if (MIXED && Aprec == 32) {
       __syncwarp();
       H_eval_jac<c64>(xJ, tJ);
@@ -1099,6 +1136,7 @@ struct PathTracker {
   // its own rounding, so it is skipped; if δ > 1e-2 the FP32 Jacobian is unusable here and
   // the path switches to FP64 (Jacobian re-evaluated and refactored at x, coefficients redone).
   __device__ HC_NI void predictor_compute(c64 t, double le0) {
+    HC_PHASE(PH_PREDICTOR);
     int m = wnum;
     c64 xi = ld(x);
     for (int attempt = 0; attempt < 2; ++attempt) {
@@ -1178,6 +1216,7 @@ struct PathTracker {
   }
   // :286-329
   __device__ HC_NI void predict(c64 t, c64 Dt) {
+    HC_PHASE(PH_PREDICT);
     if (LANE >= n) return;
     c64 xi = tx0[LANE];
     if (pmethod == PADE21) {
@@ -1250,6 +1289,7 @@ struct PathTracker {
   template <class T>
   __device__ HC_NI NewtonResult newton(c64* xbar, const c64* x0v, c64 t, double mu_, double omega_, bool ext,
                                  bool accurate_mu, bool first_correction) {
+    HC_PHASE(PH_NEWTON);
     const double a_ = ca, h_a = ch_a;
     c64 xi = ld(x0v);
     __syncwarp();
@@ -1391,6 +1431,7 @@ struct PathTracker {
     return jmin(jmin(Ds, O->max_step_size), O->max_initial_step_size);
   }
   __device__ HC_NI void update_stepsize(const NewtonResult& res) {  // :541-588
+    HC_PHASE(PH_STEPSIZE);
     double a_ = O->beta_a * O->a;
     int p = porder;
     double om = jclamp(omega + 2 * (omega - omega_prev), omega, 8 * omega);
@@ -1419,6 +1460,7 @@ struct PathTracker {
     ss.propose(Ds);
   }
   __device__ HC_NI void check_terminated() {  // :591-619
+    HC_PHASE(PH_STEPSIZE);
     double tol_acc;
     if (extended_prec || !O->extended_precision) {
       tol_acc = k_tolacc;
@@ -1488,6 +1530,7 @@ struct PathTracker {
 
   // init! (:639-754); returns is_tracking
   __device__ HC_NI bool tracker_init(c64 t1, c64 t0) {
+    HC_PHASE(PH_INIT);
     phi_valid = false;
     step_logf = 0.f;
     ds_plain_cur = 0.0;
@@ -1555,6 +1598,7 @@ struct PathTracker {
   }
   // step! (:851-926)
   __device__ HC_NI bool tracker_step() {
+    HC_PHASE(PH_STEP);
     c64 t = ss.t(), Dt = ss.Dt(), tp = ss.tp();
     const bool logging = a->log && cur_path >= a->log_lo && cur_path < a->log_hi;
     double pre[8];
@@ -1640,6 +1684,7 @@ struct PathTracker {
   // plain steps before the next learned proposal); Newton's contraction test judges every step.
   // c_learned counts proposals the network enlarged, c_learned_rej those Newton rejected.
   __device__ HC_NI void propose_next(const NewtonResult& res, c64 t_prev, bool logging, const double* pre) {
+    HC_PHASE(PH_STEPSIZE);
     const bool accepted = last_steps_failed == 0;
     acc_hist = (acc_hist << 1) | (accepted ? 1u : 0u);
     if (!accepted && step_logf > 0.f) {
@@ -2148,6 +2193,7 @@ struct PathTracker {
     return ecode;
   }
   __device__ HC_NI int eg_step() {  // :329-399
+    HC_PHASE(PH_ENDGAME);
     if (steps_eg >= O->max_endgame_steps) {
       return ecode = EC_terminated_max_steps;
     } else if (ext_steps() - ext_steps_eg_start > O->max_endgame_extended_steps) {
@@ -2193,6 +2239,7 @@ struct PathTracker {
 
   // ---------------------------------------------------------------- one path
   __device__ HC_NI void run(int64_t k) {
+    HC_PHASE(PH_RUN);
     cur_path = k;
     if (LANE < n) {
       double2 s = a->starts[k * n + LANE];

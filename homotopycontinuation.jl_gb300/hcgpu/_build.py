@@ -29,22 +29,26 @@ def _deps():
     return [f for f in files if os.path.isfile(f)]
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, defines=(), build_dir: str = BUILD) -> str:
+    """Compile and link; ``defines`` (e.g. ("HC_PHASE_CLOCKS",) for a phase-profiling
+    library) go to nvcc as -D flags, ``build_dir`` receives the objects and the library."""
+    lib = os.path.join(build_dir, "libhcgpu.so")
+    if not force and up_to_date(lib):
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     cc = nvcc()
+    dflags = [f"-D{d}" for d in defines]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(build_dir, src.replace(".cu", ".o"))
+        cmd = [cc, *ARCH, *FLAGS, *dflags, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -54,9 +58,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     r = subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib

@@ -103,8 +103,8 @@ def load(build_if_missing: bool = True):
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
-    if build_if_missing and not _build.up_to_date():
+    path = os.environ.get("HCGPU_LIB") or _build.LIB  # HCGPU_LIB: e.g. a phase-profiling build
+    if build_if_missing and path == _build.LIB and not _build.up_to_date():
         _build.build()
     if not os.path.exists(path):
         raise RuntimeError(f"libhcgpu.so not found at {path}; run __graft_entry__.build()")

@@ -234,7 +234,10 @@ class _Handle:
 
     STAT_NAMES = ["paths", "evals_jac", "evals", "evals_dd", "taylor_orders", "lu", "solves", "taylor_fp64_redo",
                   "paths_to_fp64", "monomials", "value_terms", "jacobian_terms", "blocks", "warps_per_block",
-                  "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"]
+                  "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"] + [
+        "clk_" + p for p in ("run", "step", "predictor", "predict", "newton", "eval_jac", "eval", "taylor", "lu",
+                             "solve", "norm", "stepsize", "endgame", "mono", "val_rows", "jac_rows", "refine",
+                             "init", "cond", "dd")]
 
     def stats(self):
         out = np.zeros(len(self.STAT_NAMES))

@@ -128,8 +128,18 @@ int hc_cancel(hc_handle* h);
 /* Last error message of this handle (or of the library when h is NULL). */
 const char* hc_last_error(hc_handle* h);
 
-/* Device work counters of the last call: kernel launches, evaluations, LU factorizations,
- * and the algorithmic FP64/FP32 flop counts used for the roofline (out[0..7]). */
+/* Device counters of the last tracking call on this handle, up to nout values: [0] paths,
+ * [1] evaluations with Jacobian, [2] residual-only evaluations, [3] double-double residuals,
+ * [4] Taylor orders, [5] LU factorizations, [6] triangular-solve pairs, [7] FP32 Taylor
+ * evaluations redone in FP64, [8] paths moved to FP64; [9] monomials, [10] value terms,
+ * [11] Jacobian terms of the last hc_set_homotopy program; [12] CTAs, [13] warps per CTA,
+ * [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree monomial
+ * offset; [17] learned step proposals, [18] of them rejected by Newton; [19..38] cycles per
+ * tracker phase (run, step, predictor, predict, newton, eval+Jacobian, eval, taylor, LU,
+ * solve, norm, step size, endgame, monomials, value rows, Jacobian rows, refinement, init,
+ * cond, double-double; inclusive), nonzero only in libraries built with -DHC_PHASE_CLOCKS.
+ * No counterpart in the reference (its closest analogue is the Jacobian's factorization and
+ * ldiv counters, src/linear_algebra.jl:809-862). */
 int hc_last_stats(hc_handle* h, double* out, int nout);
 
 /* Load the step-proposal network used with HC_STEP_LEARNED: `params` are the FP32 parameters
