@@ -298,6 +298,7 @@ WarpLayout make_warp_layout(const HostProg& P) {
   L.ipiv = take(32 * 4);
   L.vec = take((size_t)HC_NCVEC * vn * 16);
   L.rvec = take((size_t)HC_NRVEC * vn * 8);
+  L.v32 = take((size_t)4 * vn * 8);
   L.vn = vn;
   L.bytes = (int)off;
   return L;

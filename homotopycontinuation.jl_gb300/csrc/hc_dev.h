@@ -52,6 +52,7 @@ struct WarpLayout {
   int vec;   // complex vectors (vn elements each, 16 B)
   int rvec;  // real vectors (vn elements each, 8 B)
   int vn;    // padded vector length (elements)
+  int v32;   // FP32 staging: x (FP32 Jacobians) or tx0..tx2 (FP32 Taylor series), 4 × vn c32
 };
 constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
 constexpr int HC_NCVEC = 24, HC_NRVEC = 20;

@@ -171,7 +171,8 @@ struct PathTracker {
   char* Ab;
   char* LUb;
   c64* xJ;
-  c64* dinv;  // reciprocals of U's diagonal
+  c64* dinv;  // reciprocals of U's diagonal, stored in the LU's arithmetic (c64 or c32)
+  c32* v32;   // FP32 staging vectors (4 × vn)
   int* ipiv;
   // complex vectors
   c64 *x, *xh, *xb, *r, *s1, *s2, *s3, *tx0, *tx1, *tx2, *tx3, *ptx0, *ptx1, *u;
@@ -301,6 +302,7 @@ struct PathTracker {
     rtmp = rv + 18 * vn;
     winv = rv + 19 * vn;
     dinv = (c64*)(base + L.dinv);
+    v32 = (c32*)(base + L.v32);
     factorized = scaled = false;
     Aprec = 64;
     j64 = false;
@@ -405,10 +407,21 @@ struct PathTracker {
       __syncwarp();
     }
   }
-  __device__ HC_NI void mono_to32() {
+  // FP32 monomials for FP32 Jacobians: the chain of eval_mono64 in FP32 from x rounded once
+  // (n conversions instead of one per monomial: FP64 conversions run on the FP64 pipe)
+  __device__ HC_NI void eval_mono32(const c64* xv) {
     c32* m32 = (c32*)(mono64 + P->M);
-    for (int m = LANE; m < P->M; m += 32) m32[m] = to32(mono64[m]);
+    if (LANE < n) v32[LANE] = to32(xv[LANE]);
+    if (LANE == 0) m32[0] = C32(1.f);
     __syncwarp();
+    for (int L = 1; L < P->nlev; ++L) {
+      int b = __ldg(P->lev + L), e = __ldg(P->lev + L + 1);
+      for (int m = b + LANE; m < e; m += 32) {
+        int2 d = mdef[m];
+        m32[m] = m32[d.x] * v32[d.y];
+      }
+      __syncwarp();
+    }
   }
   // sum of the partial slots of row r
   template <class T>
@@ -432,12 +445,12 @@ struct PathTracker {
       for (; t + 4 <= g.z; t += 4) {
         int m0 = vmono[t], m1 = vmono[t + 1], m2 = vmono[t + 2], m3 = vmono[t + 3];
         c64 c0 = vcoef64[t], c1 = vcoef64[t + 1], c2 = vcoef64[t + 2], c3 = vcoef64[t + 3];
-        a0 = a0 + c0 * mono64[m0];
-        a1 = a1 + c1 * mono64[m1];
-        a2 = a2 + c2 * mono64[m2];
-        a3 = a3 + c3 * mono64[m3];
+        a0 = cfma(c0, mono64[m0], a0);
+        a1 = cfma(c1, mono64[m1], a1);
+        a2 = cfma(c2, mono64[m2], a2);
+        a3 = cfma(c3, mono64[m3], a3);
       }
-      for (; t < g.z; ++t) a0 = a0 + vcoef64[t] * mono64[vmono[t]];
+      for (; t < g.z; ++t) a0 = cfma(vcoef64[t], mono64[vmono[t]], a0);
       pp[g.w & 0xffffff] = (a0 + a1) + (a2 + a3);
     }
     __syncwarp();
@@ -473,14 +486,14 @@ struct PathTracker {
       int t = g.y;
       for (; t + 4 <= g.z; t += 4) {
         uint32_t k0 = jcode[t], k1 = jcode[t + 1], k2 = jcode[t + 2], k3 = jcode[t + 3];
-        a0 = a0 + cf[k0 >> 16] * mv[k0 & 0xffff];
-        a1 = a1 + cf[k1 >> 16] * mv[k1 & 0xffff];
-        a2 = a2 + cf[k2 >> 16] * mv[k2 & 0xffff];
-        a3 = a3 + cf[k3 >> 16] * mv[k3 & 0xffff];
+        a0 = cfma(cf[k0 >> 16], mv[k0 & 0xffff], a0);
+        a1 = cfma(cf[k1 >> 16], mv[k1 & 0xffff], a1);
+        a2 = cfma(cf[k2 >> 16], mv[k2 & 0xffff], a2);
+        a3 = cfma(cf[k3 >> 16], mv[k3 & 0xffff], a3);
       }
       for (; t < g.z; ++t) {
         uint32_t k0 = jcode[t];
-        a0 = a0 + cf[k0 >> 16] * mv[k0 & 0xffff];
+        a0 = cfma(cf[k0 >> 16], mv[k0 & 0xffff], a0);
       }
       T sum = (a0 + a1) + (a2 + a3);
       int mult = (g.w >> 24) & 0xff;
@@ -513,7 +526,7 @@ struct PathTracker {
   __device__ HC_NI void H_eval_jac(const c64* xv, c64 t) {
     HC_PHASE(PH_EVALJ);
     eval_mono64(xv);
-    if constexpr (std::is_same<T, c32>::value) mono_to32();
+    if constexpr (std::is_same<T, c32>::value) eval_mono32(xv);
     c64 F, G;
     val_rows64(F, G);
     c64 ts = gamma() * t, tt = C64(1.0) - t;
@@ -576,6 +589,12 @@ struct PathTracker {
     T* ST = S + 4 * top;
     const int lo = (K == 1) ? 0 : K - 1, hi = (K == 1) ? 0 : K;
     const c64* txv[3] = {tx0, tx1, tx2};
+    const int vn = a->L.vn;
+    if constexpr (F32) {
+      // the series inputs rounded to FP32 once (not once per monomial)
+      if (LANE < n)
+        for (int k = 0; k < K && k < 3; ++k) v32[k * vn + LANE] = to32(txv[k][LANE]);
+    }
     if (LANE == 0) {
       for (int k = 0; k < 4; ++k) {
         S[k].re = (k == 0) ? 1 : 0;
@@ -589,10 +608,14 @@ struct PathTracker {
         T X[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          if (k < K)
-            X[k] = conv<T>(txv[k][d.y]);
-          else
+          if (k < K) {
+            if constexpr (F32)
+              X[k] = v32[k * vn + d.y];
+            else
+              X[k] = txv[k][d.y];
+          } else {
             X[k].re = X[k].im = 0;
+          }
         }
         const T* Sp = S + d.x * 4;
         T c[4];
@@ -602,7 +625,7 @@ struct PathTracker {
           acc.re = acc.im = 0;
           if (k <= K) {
 #pragma unroll
-            for (int j = 0; j <= k; ++j) acc = acc + Sp[j] * X[k - j];
+            for (int j = 0; j <= k; ++j) acc = cfma(Sp[j], X[k - j], acc);
           }
           c[k] = acc;
         }
@@ -638,10 +661,10 @@ struct PathTracker {
         const T* q1 = (m1 < top) ? S + m1 * 4 + lo : ST + (m1 - top) * 2;
         int d0 = (m0 < top) ? hi - lo : 1, d1 = (m1 < top) ? hi - lo : 1;
         T v00 = q0[0], v01 = q0[d0], v10 = q1[0], v11 = q1[d1];
-        a0 = a0 + c0 * v00;
-        a1 = a1 + c0 * v01;
-        b0 = b0 + c1 * v10;
-        b1 = b1 + c1 * v11;
+        a0 = cfma(c0, v00, a0);
+        a1 = cfma(c0, v01, a1);
+        b0 = cfma(c1, v10, b0);
+        b1 = cfma(c1, v11, b1);
         if constexpr (F32) {
           float ac0 = fabsf(c0.re) + fabsf(c0.im), ac1 = fabsf(c1.re) + fabsf(c1.im);
           e0 += ac0 * (fabsf(v00.re) + fabsf(v00.im)) + ac1 * (fabsf(v10.re) + fabsf(v10.im));
@@ -654,8 +677,8 @@ struct PathTracker {
         const T* q0 = (m0 < top) ? S + m0 * 4 + lo : ST + (m0 - top) * 2;
         int d0 = (m0 < top) ? hi - lo : 1;
         T v00 = q0[0], v01 = q0[d0];
-        a0 = a0 + c0 * v00;
-        a1 = a1 + c0 * v01;
+        a0 = cfma(c0, v00, a0);
+        a1 = cfma(c0, v01, a1);
         if constexpr (F32) {
           float ac0 = fabsf(c0.re) + fabsf(c0.im);
           e0 += ac0 * (fabsf(v00.re) + fabsf(v00.im));
@@ -727,19 +750,23 @@ struct PathTracker {
   __device__ HC_NI void lu_factor_T() {  // src/linear_algebra.jl:130-184
     T* A = (T*)LUb;
     __syncwarp();
+    // pivot search in T's own precision: comparisons of FP32 magnitudes are exact, so the
+    // pivots are those of an FP64 search on the same values, without FP64 instructions
+    using R = decltype(T{}.re);
+    T* dv = (T*)dinv;  // reciprocal pivots in T
     for (int k = 0; k < n; ++k) {
-      double v = -1.0;
-      if (LANE >= k && LANE < n) v = (double)abs2(A[k * n + LANE]);
-      double vk = __shfl_sync(FULL, v, k);
+      R v = -1;
+      if (LANE >= k && LANE < n) v = abs2(A[k * n + LANE]);
+      R vk = __shfl_sync(FULL, v, k);
       int kp = k;
-      double amax = vk;
+      R amax = vk;
       if (!isnan(vk)) {
-        double bv = (LANE > k && LANE < n && !isnan(v)) ? v : -1.0;
+        R bv = (LANE > k && LANE < n && !isnan(v)) ? v : (R)-1;
         if (LANE == k) bv = vk;
         int bi = (LANE >= k && LANE < n) ? LANE : 1 << 30;
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
-          double ov = __shfl_xor_sync(FULL, bv, o);
+          R ov = __shfl_xor_sync(FULL, bv, o);
           int oi = __shfl_xor_sync(FULL, bi, o);
           if (ov > bv || (ov == bv && oi < bi)) {
             bv = ov;
@@ -750,7 +777,7 @@ struct PathTracker {
         amax = bv;
       }
       if (LANE == 0) ipiv[k] = kp;
-      if (amax != 0.0) {
+      if (amax != (R)0) {
         if (kp != k) {
           if (LANE < n) {
             T tmp = A[LANE * n + k];
@@ -766,13 +793,15 @@ struct PathTracker {
         rec.re = Akk.re * id;
         rec.im = -Akk.im * id;
         if (LANE > k && LANE < n) A[k * n + LANE] = A[k * n + LANE] * rec;
-        if (LANE == 0) dinv[k] = to64(rec);
+        if (LANE == 0) dv[k] = rec;
         __syncwarp();
       } else {
         // zero pivot column: U_kk = 0 and the solves divide by zero, as in the reference
         if (LANE == 0) {
-          T Akk = A[k * n + k];
-          dinv[k] = div_fast(C64(1.0), to64(Akk));
+          T one;
+          one.re = 1;
+          one.im = 0;
+          dv[k] = div_fast(one, A[k * n + k]);
         }
         __syncwarp();
       }
@@ -780,7 +809,7 @@ struct PathTracker {
       int tot = m * m;
       for (int e = LANE; e < tot; e += 32) {
         int i = k + 1 + e % m, j = k + 1 + e / m;
-        A[j * n + i] = A[j * n + i] - A[k * n + i] * A[j * n + k];
+        A[j * n + i] = cfms(A[k * n + i], A[j * n + k], A[j * n + i]);
       }
       __syncwarp();
     }
@@ -807,14 +836,15 @@ struct PathTracker {
         if (LANE == p) b = vi;
       }
     }
+    const T* dv = (const T*)dinv;
     for (int j = 0; j < n; ++j) {
       T xj = shfl(b, j);
-      if (LANE > j && LANE < n) b = b - A[j * n + LANE] * xj;
+      if (LANE > j && LANE < n) b = cfms(A[j * n + LANE], xj, b);
     }
     for (int j = n - 1; j >= 0; --j) {
-      if (LANE == j) b = b * conv<T>(dinv[j]);
+      if (LANE == j) b = b * dv[j];
       T xj = shfl(b, j);
-      if (LANE < j) b = b - A[j * n + LANE] * xj;
+      if (LANE < j) b = cfms(A[j * n + LANE], xj, b);
     }
     ++c_solve;
     return LANE < n ? to64(b) : C64(0.0);
@@ -824,8 +854,9 @@ struct PathTracker {
   __device__ HC_NI c64 lu_solve_adj_T(c64 b64) {
     const T* A = (const T*)LUb;
     T b = conv<T>(b64);
+    const T* dv = (const T*)dinv;
     for (int j = 0; j < n; ++j) {  // ldiv_adj_upper!
-      if (LANE == j) b = b * conj(conv<T>(dinv[j]));
+      if (LANE == j) b = b * conj(dv[j]);
       T xj = shfl(b, j);
       if (LANE > j && LANE < n) b = b - conj(A[LANE * n + j]) * xj;
     }
@@ -1679,7 +1710,8 @@ struct PathTracker {
   // After a step, the plain rule (update_stepsize!, src/tracker.jl:541-588) has proposed Δs.
   //   explore: the proposal of the next step is multiplied by f = 6^u, u uniform from a hash of
   //            (path, step) — data for training;
-  //   learned: f = exp(network(features)) ∈ [1, exp(logmax)].
+  //   learned: f = exp(network(features)) ∈ [1, exp(logmax)];
+  // both only while t > endgame_start when the endgame tracks the path (below).
   // A rejected enlarged proposal falls back to this step's plain proposal (then two accepted
   // plain steps before the next learned proposal); Newton's contraction test judges every step.
   // c_learned counts proposals the network enlarged, c_learned_rej those Newton rejected.
@@ -1695,10 +1727,14 @@ struct PathTracker {
       }
     }
     if (logging) log_step(t_prev, pre, res);
-    float logf = 0.f;
+    float lf = 0.f;
     bool valid = false;
     double dsp = ss.Ds();
-    if (accepted && !ss.is_done()) {
+    // Enlarged steps only before the endgame zone: for t < endgame_start the endgame samples
+    // the path at every step (valuation, at-infinity and singular decisions), diverging paths
+    // crowd together and the plain rule's step sequence is kept.
+    const bool zone = a->mode != 1 || ss.t().re > O->endgame_start;
+    if (accepted && !ss.is_done() && zone) {
       compute_features(res, dsp);
       valid = true;
       if (O->step_control == HC_STEP_EXPLORE) {
@@ -1706,38 +1742,38 @@ struct PathTracker {
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
         z ^= z >> 31;
-        logf = (float)((double)(z >> 11) * 0x1p-53 * 1.791759469228055);  // ln 6
+        lf = (float)(uint32_t)(z >> 40) * 0x1p-24f * 1.7917595f;  // ln 6 · u, u uniform in [0, 1)
       } else if (O->step_control == HC_STEP_LEARNED && a->model) {
         if (cooldown > 0) {
           --cooldown;
         } else {
-          logf = mlp_logf();
+          lf = mlp_logf();
         }
       }
     }
-    if (logf > 0.f) {
+    if (lf > 0.f) {
       // an enlarged step stays within 0.75 τ (β_τ of the reference's "fast" parameters,
       // src/tracker.jl:58-62), never below the plain proposal; the applied multiplier is kept
-      double ds = jmin(dsp * exp((double)logf), jmax(dsp, 0.75 * tau));
+      double ds = jmin(dsp * (double)expf(lf), jmax(dsp, 0.75 * tau));
       ss.propose(ds);
-      logf = (float)log(ss.Ds() / dsp);
-      if (!(logf > 0.f)) {
-        logf = 0.f;
+      lf = logf((float)(ss.Ds() / dsp));
+      if (!(lf > 0.f)) {
+        lf = 0.f;
         ss.propose(dsp);
       } else if (O->step_control == HC_STEP_LEARNED) {
         ++c_learned;
       }
     }
     phi_valid = valid;
-    step_logf = logf;
+    step_logf = lf;
     ds_plain_cur = dsp;
   }
   // the 12 features of the step that was just accepted (all lanes hold the same values)
   __device__ HC_NI void compute_features(const NewtonResult& res, double dsp) {
-    auto lg = [](double v) -> float {
-      double l = log10(v);
+    auto lg = [](double v) -> float {  // FP32 log: features are FP32 and clamped to ±40
+      float l = log10f((float)v);
       if (!(l == l)) return 0.f;
-      return (float)fmin(40.0, fmax(-40.0, l));
+      return fminf(40.f, fmaxf(-40.f, l));
     };
     double xnorm = vnorm(ld(x), nullptr);
     phi[0] = (float)ss.t().re;
@@ -1747,7 +1783,8 @@ struct PathTracker {
     phi[4] = lg(local_error);
     phi[5] = lg(xnorm);
     phi[6] = lg(omega);
-    phi[7] = lg(dsp / tau);
+    phi[7] = lg(dsp) - lg(tau);
+    if (fabsf(phi[7]) >= 40.f || fabsf(lg(dsp)) >= 40.f || fabsf(lg(tau)) >= 40.f) phi[7] = lg(dsp / tau);
     phi[8] = (float)__popc(acc_hist & 0xffu) * 0.125f;
     phi[9] = (float)res.iters * 0.25f;
     phi[10] = lg(mu);

@@ -44,6 +44,21 @@ __device__ __forceinline__ c32 C32(float r, float i = 0.f) { return c32{r, i}; }
 HC_COMPLEX_OPS(c64, double)
 HC_COMPLEX_OPS(c32, float)
 
+// acc + a·b and acc − a·b with two fused multiply-adds per component (4 per complex op;
+// the operator form compiles to a multiply, a multiply-add and an add per component)
+__device__ __forceinline__ c64 cfma(c64 a, c64 b, c64 acc) {
+  return c64{fma(a.re, b.re, fma(-a.im, b.im, acc.re)), fma(a.re, b.im, fma(a.im, b.re, acc.im))};
+}
+__device__ __forceinline__ c32 cfma(c32 a, c32 b, c32 acc) {
+  return c32{fmaf(a.re, b.re, fmaf(-a.im, b.im, acc.re)), fmaf(a.re, b.im, fmaf(a.im, b.re, acc.im))};
+}
+__device__ __forceinline__ c64 cfms(c64 a, c64 b, c64 acc) {
+  return c64{fma(-a.re, b.re, fma(a.im, b.im, acc.re)), fma(-a.re, b.im, fma(-a.im, b.re, acc.im))};
+}
+__device__ __forceinline__ c32 cfms(c32 a, c32 b, c32 acc) {
+  return c32{fmaf(-a.re, b.re, fmaf(a.im, b.im, acc.re)), fmaf(-a.re, b.im, fmaf(-a.im, b.re, acc.im))};
+}
+
 __device__ __forceinline__ double fast_abs(c64 a) { return sqrt(abs2(a)); }
 __device__ __forceinline__ double cabs(c64 a) { return hypot(a.re, a.im); }
 __device__ __forceinline__ bool isnanc(c64 a) { return isnan(a.re) || isnan(a.im); }
