@@ -2,6 +2,7 @@
 homotopy (59,049 paths), with the plain FP64 GPU tracker and the CPU oracle beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload dense|sparse|uneven]
 
 A "step" is one batched tracking call over all paths of the workload. Prints one JSON line.
 Under torchrun (N > 1) every rank tracks its own seeded instance (weak scaling) and rank 0
@@ -28,6 +29,13 @@ sys.path.insert(0, os.path.join(ROOT, "homotopycontinuation.jl_gb300"))
 METRIC = "paths/sec at ≤1e-10 rel endpoint err: learned vs plain step control, 1 GB300"
 N_VARS, DEGREE = 10, 3
 WORKLOAD = "total-degree homotopy, 10 dense cubics in 10 complex variables (286 monomials each), 59,049 paths"
+WORKLOADS = {
+    "dense": WORKLOAD,
+    "sparse": "total-degree homotopy, 8 sparse polynomials in 8 complex variables (8 random monomials of degree "
+              "<= 4 plus a constant each), 65,536 paths, most diverging (endgame-heavy)",
+    "uneven": "2,000 independent dense instances in one launch, n uniform in 3..8, each equation degree uniform "
+              "in {2,3}, all total-degree paths of every instance",
+}
 
 
 def parse():
@@ -42,13 +50,18 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--paths", type=int, default=0, help="track only the first N paths (profiling cases)")
+    p.add_argument("--workload", default="dense", choices=list(WORKLOADS),
+                   help="dense: the headline workload; sparse and uneven: the endgame-heavy and batched cases")
     return p.parse_args()
 
 
-def workload(seed):
+def workload(seed, kind="dense"):
     import hcgpu as hc
 
-    F, g = hc.dense_random_system(N_VARS, DEGREE, seed=seed)
+    if kind == "sparse":
+        F, g = hc.sparse_random_system(8, 8, 4, seed=seed)
+    else:
+        F, g = hc.dense_random_system(N_VARS, DEGREE, seed=seed)
     H = hc.total_degree_homotopy(F, g)
     S = hc.total_degree_start_solutions(H.degrees)
     return H, S
@@ -153,7 +166,11 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    H, S = workload(args.seed)
+    if args.workload == "uneven":
+        print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable": "the reference CPU arm is timed on "
+                          "the dense headline workload only"}), flush=True)
+        return
+    H, S = workload(args.seed, args.workload)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import hco
 
@@ -176,7 +193,7 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded complex Gaussian coefficients)",
         "impl": "reference",
-        "config": {"workload": WORKLOAD, "seed": args.seed, "sample_paths": sample},
+        "config": {"workload": WORKLOADS[args.workload], "seed": args.seed, "sample_paths": sample},
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port",
                          "sample": f"{sample} evenly spaced paths of {len(S)} per step; HomotopyContinuation.jl needs "
                                    f"Julia (not installed), so the C++ restatement of its tracker runs instead"},
@@ -204,7 +221,9 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    H, S = workload(args.seed + rank)
+    if args.workload == "uneven":
+        return main_uneven(args, torch, hc, _lib, local)
+    H, S = workload(args.seed + rank, args.workload)
     if args.paths:
         S = S[: args.paths]
     npaths, n = S.shape
@@ -319,7 +338,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128",
             "data": "synthetic (seeded complex Gaussian coefficients, N(0,1/2) re/im)",
-            "config": {"workload": WORKLOAD, "seed": args.seed, "paths_per_gpu": npaths, "n": n, "degree": DEGREE,
+            "config": {"workload": WORKLOADS[args.workload], "seed": args.seed, "paths_per_gpu": npaths, "n": n,
                        "precision": args.precision, "step_control": args.step_control,
                        "l2": "256 MiB buffer written between timed steps (inputs are smaller than L2)",
                        "parallelism": f"weak: one seeded instance per GPU x{world}",
@@ -350,6 +369,115 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def main_uneven(args, torch, hc, _lib, local):
+    """The batched workload: 2,000 uneven instances tracked by one persistent launch per step
+    (hc_track_batch_device, recorded once in a CUDA graph), with the plain FP64 batch beside it."""
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        raise SystemExit("--workload uneven runs on one GPU")
+    inst = hc.uneven_instances(2000, args.seed)
+    Hs = [hc.total_degree_homotopy(F, g) for F, g in inst]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    L = _lib.load()
+
+    def batch(precision, step_control):
+        return hc.BatchTracker(Hs, hc.TrackerOptions(precision=precision, step_control=step_control))
+
+    B = batch(args.precision, args.step_control)
+    S = B.start_solutions()
+    d_starts = torch.from_numpy(S.view(np.float64)).to(dev)
+    d_res = torch.empty(B.total_paths * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    d_sol = torch.empty(2 * B.total_elements, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def device_call(Bt):
+        rc = L.hc_track_batch_device(Bt._h.h, ct.c_void_p(d_starts.data_ptr()), 1, ct.c_void_p(d_res.data_ptr()),
+                                     ct.c_void_p(d_sol.data_ptr()), ct.c_void_p(stream.cuda_stream))
+        _lib.check(rc, Bt._h.h)
+
+    def timed(Bt, steps, warmup):
+        for _ in range(warmup):
+            device_call(Bt)
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            device_call(Bt)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
+    def results():
+        r = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+        return r, d_sol.cpu().numpy().view(np.complex128)
+
+    def counts(r):
+        rc = r["return_code"]
+        return {"nonsingular": int(((rc == 1) & (r["singular"] == 0)).sum()),
+                "singular": int(((rc == 1) & (r["singular"] == 1)).sum()),
+                "at_infinity": int(np.isin(rc, [2, 3]).sum()), "failed": int((~np.isin(rc, [1, 2, 3])).sum())}
+
+    with ClockSampler(local) as clk:
+        times = timed(B, args.steps, args.warmup)
+    stats = B.stats()
+    res, sol = results()
+    ms = float(np.mean(times))
+    B64 = batch("fp64", "plain")
+    t64 = timed(B64, 1, 1)
+    res64, sol64 = results()
+    nvec = np.repeat(B.n, B.npaths)
+    ok = (res["return_code"] == 1) & (res64["return_code"] == 1) & (res["singular"] == 0) & (res64["singular"] == 0)
+    off = np.concatenate([[0], np.cumsum(nvec)])[:-1]
+    err = 0.0
+    for k in np.nonzero(ok)[0]:
+        a, b = sol[off[k]:off[k] + nvec[k]], sol64[off[k]:off[k] + nvec[k]]
+        err = max(err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+    # end to end through the host API
+    out_res = np.zeros(B.total_paths, dtype=_lib.RESULT_DTYPE)
+    out_sol = np.zeros(B.total_elements, dtype=np.complex128)
+    pinned = torch.from_numpy(S.view(np.float64)).pin_memory().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _lib.check(L.hc_track_batch(B._h.h, pinned.ctypes.data_as(ct.c_void_p), 1, out_res.ctypes.data_as(ct.c_void_p),
+                                out_sol.ctypes.data_as(ct.c_void_p)), B._h.h)
+    e2e_s = time.perf_counter() - t0
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": B.total_paths / (ms / 1000), "unit": "paths/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": "synthetic (seeded complex Gaussian coefficients, N(0,1/2) re/im)",
+            "config": {"workload": WORKLOADS["uneven"], "seed": args.seed, "instances": len(Hs),
+                       "paths": B.total_paths, "precision": args.precision, "step_control": args.step_control,
+                       "ctas": stats["blocks"], "warps_per_cta": stats["warps_per_block"],
+                       "l2": "256 MiB buffer written between timed steps"},
+            "e2e": {"value": B.total_paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(S.nbytes),
+                    "d2h_bytes_per_step": int(out_res.nbytes + out_sol.nbytes)},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "roofline": None,
+            "cpu_baseline": None,
+            "plain_fp64_gpu": {"value": B.total_paths / (float(np.mean(t64)) / 1000), "unit": "paths/s",
+                               "counts": counts(res64)},
+            "speedup_vs_plain_fp64_gpu": float(np.mean(t64)) / ms,
+            "counts": counts(res),
+            "counts_identical_to_fp64": counts(res) == counts(res64),
+            "codes_differing_from_fp64": int((res["return_code"] != res64["return_code"]).sum()),
+            "max_rel_endpoint_err_vs_fp64_gpu": err,
+            "steps_per_path": float((res["accepted_steps"] + res["rejected_steps"]).mean()),
+            "steps_per_path_plain_fp64": float((res64["accepted_steps"] + res64["rejected_steps"]).mean()),
+        }
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -708,19 +708,26 @@ struct PathTracker {
       out[LANE] = uu;
       if constexpr (F32) {
         const float* pe = (const float*)(pp + 2 * R.nslots);
+        // the bound in FP32 (a magnitude estimate; FP64 adds would run on the FP64 pipe)
         auto asum = [&](const float* e, int rr) {
-          double acc = 0.0;
+          float acc = 0.f;
           for (int k = __ldg(R.row_slot + rr); k < __ldg(R.row_slot + rr + 1); ++k) acc += e[k];
           return acc;
         };
-        double AF0 = asum(pe, LANE), AF1 = asum(pe + R.nslots, LANE);
-        double AG0 = asum(pe, n + LANE), AG1 = asum(pe + R.nslots, n + LANE);
-        double gab = cabs(gamma());
-        double bound = (K == 1) ? gab * AG0 + AF0 : gab * (AG0 + cabs(t) * AG1) + cabs(C64(1.0) - t) * AF1 + AF0;
-        bound *= 0x1p-21;
-        double au = cabs(uu);
-        ratio = (au > 0.0) ? bound / au : (bound > 0.0 ? dINF() : 0.0);
-        if (isnan(ratio)) ratio = dINF();
+        float AF0 = asum(pe, LANE), AF1 = asum(pe + R.nslots, LANE);
+        float AG0 = asum(pe, n + LANE), AG1 = asum(pe + R.nslots, n + LANE);
+        float gab = sqrtf((float)abs2(gamma()));
+        float bound;
+        if (K == 1) {
+          bound = gab * AG0 + AF0;
+        } else {
+          float at = sqrtf((float)abs2(t)), a1t = sqrtf((float)abs2(C64(1.0) - t));
+          bound = gab * (AG0 + at * AG1) + a1t * AF1 + AF0;
+        }
+        bound *= 0x1p-21f;
+        float au = sqrtf((float)abs2(uu));
+        float rf = (au > 0.f) ? bound / au : (bound > 0.f ? __int_as_float(0x7f800000) : 0.f);
+        ratio = isnan(rf) ? dINF() : (double)rf;
       }
     }
     __syncwarp();
@@ -891,6 +898,36 @@ struct PathTracker {
   // skeel_row_scaling! (:432-459) of the current A with column weights c
   __device__ HC_NI void skeel_row_scaling(double* d, const double* c, double thr) {
     __syncwarp();
+    // 2^-e as a bit pattern (exact; exp2 would run on the FP64 pipe)
+    auto pow2neg = [](int e) -> double {
+      int b = 1023 - e;
+      return (b >= 1 && b <= 2046) ? __longlong_as_double((long long)b << 52) : exp2((double)-e);
+    };
+    // FP32 Jacobians with weights in FP32 range: the row sums in FP32 (only their binary
+    // exponents are used); otherwise in FP64
+    const double cl = LANE < n ? c[LANE] : 1.0;
+    if (Aprec == 32 && __all_sync(FULL, cl > 1e-30 && cl < 1e30)) {
+      const c32* A32 = (const c32*)Ab;
+      const float cf = (float)cl;
+      float di = 0.f;
+      for (int j = 0; j < n; ++j) {
+        float cj = __shfl_sync(FULL, cf, j);
+        if (LANE < n) {
+          c32 a = A32[j * n + LANE];
+          di = fmaf(hypotf(a.re, a.im), cj, di);
+        }
+      }
+      float m = wjmaxf(di, LANE, n);
+      float sth = (float)thr + m;
+      if (LANE < n) {
+        int e = 0;
+        frexpf(di, &e);
+        if (!isfinite(di)) e = 0;
+        d[LANE] = ((float)e < sth) ? 1.0 : pow2neg(e);
+      }
+      __syncwarp();
+      return;
+    }
     double di = 0.0;
     if (LANE < n)
       for (int j = 0; j < n; ++j) {
@@ -904,7 +941,7 @@ struct PathTracker {
       int e = 0;
       frexp(di, &e);
       if (!isfinite(di)) e = 0;
-      d[LANE] = (e < s) ? 1.0 : exp2((double)-e);
+      d[LANE] = (e < s) ? 1.0 : pow2neg(e);
     }
     __syncwarp();
   }
@@ -915,8 +952,12 @@ struct PathTracker {
       c64* LU = (c64*)LUb;
       for (int e = LANE; e < nn; e += 32) LU[e] = LU[e] * rs[e % n];
     } else {
+      // the scale factors rounded to FP32 once (staged in the fourth FP32 vector)
+      float* rsf = (float*)(v32 + 3 * a->L.vn);
+      if (LANE < n) rsf[LANE] = (float)rs[LANE];
+      __syncwarp();
       c32* LU = (c32*)LUb;
-      for (int e = LANE; e < nn; e += 32) LU[e] = LU[e] * (float)rs[e % n];
+      for (int e = LANE; e < nn; e += 32) LU[e] = LU[e] * rsf[e % n];
     }
     scaled = true;
     __syncwarp();

@@ -213,5 +213,16 @@ __device__ __forceinline__ double wjmax(double d, int lane, int n) {
   if (anynan) return dNaN();
   return wmax_plain(lane < n ? d : -dINF());
 }
+__device__ __forceinline__ float wjmaxf(float d, int lane, int n) {
+  unsigned anynan = __ballot_sync(FULL, lane < n && isnan(d));
+  if (anynan) return __int_as_float(0x7fc00000);
+  float v = lane < n ? d : -__int_as_float(0x7f800000);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    float u = __shfl_xor_sync(FULL, v, o);
+    v = u > v ? u : v;
+  }
+  return v;
+}
 
 }  // namespace hcd

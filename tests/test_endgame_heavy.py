@@ -1,0 +1,86 @@
+"""GPU tests on the endgame-heavy workload: 8 sparse polynomials in 8 variables (8 random
+monomials of degree ≤ 4 plus a constant each), 65,536 total-degree paths, most diverging.
+
+On such paths the endgame's at-infinity / finite decision is ill-conditioned: for paths whose
+norm reaches 1e4..1e11, perturbations at the rounding level (a different step sequence, FP32
+Jacobians) can change the outcome between at_infinity, terminated_max_extended_steps and a
+huge "success". The learned step proposal (which only acts before the endgame zone) must not
+change anything else: every path that ends at a moderate-norm solution in either run has the
+same code and endpoint in both, and no solution is found twice (path jumping)."""
+import numpy as np
+import pytest
+
+import hcgpu as hc
+from _parity import REL_TOL, rel_err
+from hcgpu import learn
+
+pytestmark = pytest.mark.gpu
+
+BIG = 1e3  # ‖x‖∞ from which a path counts as diverging
+
+
+def _system():
+    F, g = hc.sparse_random_system(8, 8, 4, seed=0)
+    H = hc.total_degree_homotopy(F, g)
+    return H, hc.total_degree_start_solutions(H.degrees)
+
+
+def _duplicates(r, x):
+    ok = (r["return_code"] == 1) & (r["singular"] == 0)
+    X = x[ok]
+    key = np.round(X / np.maximum(np.abs(X).max(1, keepdims=True), 1e-300), 8)
+    _, counts = np.unique(key.view(np.complex128).reshape(len(X), -1), axis=0, return_counts=True)
+    return int((counts > 1).sum())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_learned_steps_on_endgame_heavy_system(precision):
+    H, S = _system()
+    model = learn.default_model()
+    r0, x0, _, _ = hc.EndgameTracker(H, hc.TrackerOptions(precision="fp64")).track_arrays(S)
+    T = hc.EndgameTracker(H, hc.TrackerOptions(precision=precision, step_control="learned", step_model=model))
+    r1, x1, _, _ = T.track_arrays(S)
+    assert T.stats()["learned_proposals"] > 0
+    n0 = np.abs(x0).max(1)
+    n1 = np.abs(x1).max(1)
+    moderate = ((r0["return_code"] == 1) & (n0 < BIG)) | ((r1["return_code"] == 1) & (n1 < BIG))
+    assert moderate.sum() > 30000
+    assert (r0["return_code"][moderate] == r1["return_code"][moderate]).all()
+    assert (r0["singular"][moderate] == r1["singular"][moderate]).all()
+    both = moderate & (r0["singular"] == 0)
+    assert rel_err(x1[both], x0[both]).max() <= REL_TOL
+    # code changes only on diverging paths, and only a handful
+    diff = r0["return_code"] != r1["return_code"]
+    assert (np.minimum(n0, n1)[diff] >= BIG).all()
+    assert diff.sum() <= 16
+    # no path jumping: no nonsingular solution found twice
+    assert _duplicates(r1, x1) == _duplicates(r0, x0) == 0
+    # fewer steps
+    s0 = (r0["accepted_steps"] + r0["rejected_steps"]).sum()
+    s1 = (r1["accepted_steps"] + r1["rejected_steps"]).sum()
+    assert s1 <= 0.8 * s0
+
+
+def test_fp64_tracker_against_oracle_on_endgame_heavy_system():
+    """All 65,536 paths against the CPU oracle: nonsingular and singular counts identical, every
+    moderate-norm outcome identical (codes, nonsingular endpoints within 1e-10); diverging paths
+    may differ only between at_infinity and the failure codes of an exhausted step budget, and
+    the total of at_infinity + failed is identical."""
+    from _parity import counts, oracle_track
+
+    H, S = _system()
+    ro, xo, _, _ = oracle_track(H, S)
+    rg, xg, _, _ = hc.EndgameTracker(H, hc.TrackerOptions(precision="fp64")).track_arrays(S)
+    co, cg = counts(ro), counts(rg)
+    assert co["nonsingular"] == cg["nonsingular"] and co["singular"] == cg["singular"]
+    assert co["at_infinity"] + co["failed"] == cg["at_infinity"] + cg["failed"]
+    assert abs(co["at_infinity"] - cg["at_infinity"]) <= 4
+    no, ng = np.abs(xo).max(1), np.abs(xg).max(1)
+    moderate = ((ro["return_code"] == 1) & (no < BIG)) | ((rg["return_code"] == 1) & (ng < BIG))
+    assert (ro["return_code"][moderate] == rg["return_code"][moderate]).all()
+    both = moderate & (ro["singular"] == 0) & (rg["singular"] == 0)
+    assert rel_err(xg[both], xo[both]).max() <= REL_TOL
+    diff = ro["return_code"] != rg["return_code"]
+    assert diff.sum() <= 16
+    assert (np.minimum(no, ng)[diff] >= BIG).all()
+    assert set(np.unique(ro["return_code"][diff])) | set(np.unique(rg["return_code"][diff])) <= {2, 4, 8, 9}
