@@ -313,6 +313,7 @@ def main():
         _lib.check(rc, T._h.h)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = float(np.mean(e2e_times))
+    retracked = int(T.stats()["paths_retracked"])
     if dist:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -358,6 +359,7 @@ def main():
             "counts": counts(res),
             "counts_identical_to_fp64": counts(res) == counts(res64),
             "max_rel_endpoint_err_vs_fp64_gpu": float(rel.max()) if len(rel) else None,
+            "paths_retracked_by_jump_check": retracked,
             "max_rel_endpoint_err_vs_oracle_sample": rel_oracle,
             "codes_identical_to_oracle_sample": codes_equal,
             "device_counters": {k: stats[k] for k in ["evals_jac", "evals", "evals_dd", "taylor_orders", "lu",
@@ -436,13 +438,18 @@ def main_uneven(args, torch, hc, _lib, local):
     t64 = timed(B64, 1, 1)
     res64, sol64 = results()
     nvec = np.repeat(B.n, B.npaths)
-    ok = (res["return_code"] == 1) & (res64["return_code"] == 1) & (res["singular"] == 0) & (res64["singular"] == 0)
     off = np.concatenate([[0], np.cumsum(nvec)])[:-1]
-    err = 0.0
-    for k in np.nonzero(ok)[0]:
-        a, b = sol[off[k]:off[k] + nvec[k]], sol64[off[k]:off[k] + nvec[k]]
-        err = max(err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
-    # end to end through the host API
+
+    def max_err(r, x):
+        ok = (r["return_code"] == 1) & (res64["return_code"] == 1) & (r["singular"] == 0) & (res64["singular"] == 0)
+        e = 0.0
+        for k in np.nonzero(ok)[0]:
+            a, b = x[off[k]:off[k] + nvec[k]], sol64[off[k]:off[k] + nvec[k]]
+            e = max(e, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+        return e
+
+    err_device = max_err(res, sol)
+    # end to end through the host API (which also re-tracks jumped paths, see hc_track_batch)
     out_res = np.zeros(B.total_paths, dtype=_lib.RESULT_DTYPE)
     out_sol = np.zeros(B.total_elements, dtype=np.complex128)
     pinned = torch.from_numpy(S.view(np.float64)).pin_memory().numpy()
@@ -451,6 +458,8 @@ def main_uneven(args, torch, hc, _lib, local):
     _lib.check(L.hc_track_batch(B._h.h, pinned.ctypes.data_as(ct.c_void_p), 1, out_res.ctypes.data_as(ct.c_void_p),
                                 out_sol.ctypes.data_as(ct.c_void_p)), B._h.h)
     e2e_s = time.perf_counter() - t0
+    retracked = int(B.stats()["paths_retracked"])
+    err = max_err(out_res, out_sol)
     if rank == 0:
         line = {
             "metric": METRIC, "value": B.total_paths / (ms / 1000), "unit": "paths/s", "n_gpus": 1,
@@ -470,10 +479,12 @@ def main_uneven(args, torch, hc, _lib, local):
             "plain_fp64_gpu": {"value": B.total_paths / (float(np.mean(t64)) / 1000), "unit": "paths/s",
                                "counts": counts(res64)},
             "speedup_vs_plain_fp64_gpu": float(np.mean(t64)) / ms,
-            "counts": counts(res),
-            "counts_identical_to_fp64": counts(res) == counts(res64),
-            "codes_differing_from_fp64": int((res["return_code"] != res64["return_code"]).sum()),
+            "counts": counts(out_res),
+            "counts_identical_to_fp64": counts(out_res) == counts(res64),
+            "codes_differing_from_fp64": int((out_res["return_code"] != res64["return_code"]).sum()),
             "max_rel_endpoint_err_vs_fp64_gpu": err,
+            "paths_retracked_by_jump_check": retracked,
+            "max_rel_endpoint_err_device_call_unchecked": err_device,
             "steps_per_path": float((res["accepted_steps"] + res["rejected_steps"]).mean()),
             "steps_per_path_plain_fp64": float((res64["accepted_steps"] + res64["rejected_steps"]).mean()),
         }

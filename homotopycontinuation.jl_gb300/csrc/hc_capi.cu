@@ -403,6 +403,15 @@ struct hc_handle {
   int bgraph_endgame = -1, bgraph_blocks = 0, bgraph_wpc = 0;
   unsigned long long bgraph_gen = 0;
   unsigned long long generation = 1;  // bumped whenever options, model or batch change
+  std::vector<int64_t> bpath_off, bvec_off, bnpaths;  // host copies of the batch's instance offsets
+  std::vector<int> bn;
+  // jump check of the host entry points (learned step control)
+  int64_t* d_plist = nullptr;
+  size_t plist_cap = 0;
+  BatchUnit* d_runits = nullptr;
+  size_t runits_cap = 0;
+  double retracked = 0;     // paths re-tracked with plain step control by the last host call
+  bool stats_on_host = false;  // the last call was a host entry point: its counters are final
   int last_blocks = 0, last_wpc = 0;
   cudaStream_t last_stream = nullptr;
   // step log
@@ -509,6 +518,8 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_binst[0]);
   cudaFree(h->d_binst[1]);
   cudaFree(h->d_bunits);
+  cudaFree(h->d_plist);
+  cudaFree(h->d_runits);
   if (h->bgraph) cudaGraphExecDestroy(h->bgraph);
   cudaFree(h->d_log);
   cudaFree(h->d_log_count);
@@ -593,6 +604,11 @@ static int ensure_capacity_v(hc_handle* h, int64_t npaths, int64_t nvec) {
 }
 static int ensure_capacity(hc_handle* h, int64_t npaths, int n) { return ensure_capacity_v(h, npaths, npaths * n); }
 
+static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
+                             double t1_im, double t0_re, double t0_im, hc_path_result* d_results,
+                             double* d_solutions, double* d_valuation, double* d_last, cudaStream_t s,
+                             const hc_options& O, const int64_t* d_path_list);
+
 int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
                     double t1_im, double t0_re, double t0_im, hc_path_result* d_results, double* d_solutions,
                     double* d_valuation, double* d_last, void* stream) {
@@ -604,11 +620,22 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   if (h->opts.step_control == HC_STEP_LEARNED && !h->d_model)
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: learned step control needs hc_set_step_model");
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  h->stats_on_host = false;
+  return track_device_impl(h, npaths, d_starts, endgame, t1_re, t1_im, t0_re, t0_im, d_results, d_solutions,
+                           d_valuation, d_last, s, h->opts, nullptr);
+}
+
+// one launch of the tracking kernel with options O; with d_path_list, queue item i tracks path
+// d_path_list[i] in place (results and endpoints at that path's own index)
+static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
+                             double t1_im, double t0_re, double t0_im, hc_path_result* d_results,
+                             double* d_solutions, double* d_valuation, double* d_last, cudaStream_t s,
+                             const hc_options& O, const int64_t* d_path_list) {
   Launch la{};
   la.P = h->dprog;
-  la.O = h->opts;
+  la.O = O;
   la.L = h->layout;
-  la.T = make_table_layout(h->prog, h->opts.precision);
+  la.T = make_table_layout(h->prog, O.precision);
   la.npaths = npaths;
   la.starts = (const double2*)d_starts;
   la.res = d_results;
@@ -628,12 +655,13 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   la.log_cap = h->log_cap;
   la.log_lo = h->log_lo;
   la.log_hi = h->log_hi;
-  la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+  la.model = O.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
   la.phase = h->d_counter + 1 + HC_NSTATS;
+  la.path_list = d_path_list;
   if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
   // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
   const size_t smem_cap = 227 * 1024;
-  int wpc = h->opts.warps_per_cta;
+  int wpc = O.warps_per_cta;
   if (wpc <= 0) {
     wpc = (int)std::min<size_t>(8, (smem_cap - la.T.bytes) / la.L.bytes);
     wpc = std::max(wpc, 1);
@@ -644,9 +672,9 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
     smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
   }
   int bps = 0;
-  CK(occupancy(h->opts.precision, wpc, smem, &bps));
+  CK(occupancy(O.precision, wpc, smem, &bps));
   if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_device: kernel does not fit on an SM");
-  if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
+  if (O.ctas_per_sm > 0) bps = std::min(bps, O.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
   CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), s));
@@ -655,6 +683,42 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
   h->last_wpc = wpc;
   h->last_stream = s;
   return HC_OK;
+}
+
+// Jump check of the host entry points with learned step control. A path that jumps onto
+// another path ends at that path's solution: two nonsingular endpoints coincide. Returns the
+// paths (indices into res/sol) whose nonsingular endpoints coincide with another's within
+// rtol·max(‖x‖∞, 1) — the candidates are swept in order of their first coordinate scaled by
+// ‖x‖∞, which coincident endpoints share up to rounding.
+static std::vector<int64_t> coincident_paths(const hc_path_result* res, const double2* sol, int64_t npaths, int n,
+                                             double rtol = 1e-8) {
+  struct C {
+    double key, norm;
+    int64_t k;
+  };
+  std::vector<C> c;
+  for (int64_t k = 0; k < npaths; ++k) {
+    if (res[k].return_code != 1 || res[k].singular) continue;  // EndgameTrackerCode success
+    const double2* x = sol + k * n;
+    double m = 0;
+    for (int i = 0; i < n; ++i) m = std::max(m, std::max(std::fabs(x[i].x), std::fabs(x[i].y)));
+    if (!std::isfinite(m)) continue;
+    c.push_back({x[0].x / std::max(m, 1e-300), m, k});
+  }
+  std::sort(c.begin(), c.end(), [](const C& a, const C& b) { return a.key < b.key; });
+  std::vector<char> mark(npaths, 0);
+  for (size_t a = 0; a < c.size(); ++a)
+    for (size_t b = a + 1; b < c.size() && c[b].key - c[a].key <= 4 * rtol; ++b) {
+      const double2* xa = sol + c[a].k * n;
+      const double2* xb = sol + c[b].k * n;
+      double tol = rtol * std::max(std::max(c[a].norm, c[b].norm), 1.0), d = 0;
+      for (int i = 0; i < n && d <= tol; ++i) d = std::max(d, std::max(std::fabs(xa[i].x - xb[i].x), std::fabs(xa[i].y - xb[i].y)));
+      if (d <= tol) mark[c[a].k] = mark[c[b].k] = 1;
+    }
+  std::vector<int64_t> out;
+  for (int64_t k = 0; k < npaths; ++k)
+    if (mark[k]) out.push_back(k);
+  return out;
 }
 
 int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, double t1_re, double t1_im,
@@ -684,7 +748,47 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
+  h->retracked = 0;
+  h->stats_on_host = true;
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
+  if (h->opts.step_control == HC_STEP_LEARNED && endgame) {
+    // re-track the paths whose endpoints coincide with plain step control, in place
+    std::vector<int64_t> idx = coincident_paths(out_results, (const double2*)out_solutions, npaths, n);
+    if (!idx.empty()) {
+      if (h->plist_cap < idx.size()) {
+        cudaFree(h->d_plist);
+        h->d_plist = nullptr;
+        h->plist_cap = 0;
+        CK(cudaMalloc(&h->d_plist, idx.size() * sizeof(int64_t)));
+        h->plist_cap = idx.size();
+      }
+      CK(cudaMemcpyAsync(h->d_plist, idx.data(), idx.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+      hc_options O = h->opts;
+      O.step_control = HC_STEP_PLAIN;
+      rc = track_device_impl(h, (int64_t)idx.size(), (const double*)h->d_starts, endgame, t1_re, t1_im, t0_re,
+                             t0_im, h->d_res, (double*)h->d_sol, h->d_val, (double*)h->d_last, h->stream, O,
+                             h->d_plist);
+      if (rc != HC_OK) return rc;
+      for (int64_t k : idx) {
+        CK(cudaMemcpyAsync(out_results + k, h->d_res + k, sizeof(hc_path_result), cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaMemcpyAsync(out_solutions + 2 * k * n, h->d_sol + k * n, n * sizeof(double2),
+                           cudaMemcpyDeviceToHost, h->stream));
+        if (out_valuation)
+          CK(cudaMemcpyAsync(out_valuation + k * n, h->d_val + k * n, n * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+        if (out_last)
+          CK(cudaMemcpyAsync(out_last + 2 * k * n, h->d_last + k * n, n * sizeof(double2), cudaMemcpyDeviceToHost,
+                             h->stream));
+      }
+      CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] += (double)st[i];
+      h->stats[0] -= (double)idx.size();  // paths: counted once
+      h->retracked = (double)idx.size();
+      if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
+    }
+  }
   return HC_OK;
 }
 
@@ -886,11 +990,72 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, con
   h->bwstride = ws;
   h->btotal_paths = tp;
   h->btotal_vec = tv;
+  h->bpath_off.resize(ninstances);
+  h->bvec_off.resize(ninstances);
+  h->bnpaths.resize(ninstances);
+  h->bn.resize(ninstances);
+  for (int i = 0; i < ninstances; ++i) {
+    h->bpath_off[i] = I[0][i].path_off;
+    h->bvec_off[i] = I[0][i].vec_off;
+    h->bnpaths[i] = inst[i].npaths;
+    h->bn[i] = inst[i].n;
+  }
   h->has_batch = true;
   ++h->generation;
   if (total_paths) *total_paths = tp;
   if (total_elements) *total_elements = tv;
   return HC_OK;
+}
+
+// shared memory, warps per CTA and CTAs of a batch launch with options O
+static int batch_geometry(hc_handle* h, const hc_options& O, int nunits, size_t* smem_out, int* wpc_out,
+                          int* blocks_out) {
+  const int q = O.precision == HC_PREC_MIXED ? 1 : 0;
+  const size_t smem_cap = 227 * 1024;
+  const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
+  int wpc = O.warps_per_cta;
+  if (wpc <= 0) wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride));
+  size_t smem = fixed + (size_t)wpc * h->bwstride;
+  while (wpc > 1 && smem > smem_cap) {
+    --wpc;
+    smem = fixed + (size_t)wpc * h->bwstride;
+  }
+  if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "batch: working set exceeds shared memory");
+  int bps = 0;
+  CK(prepare_batch(O.precision, smem, wpc, &bps));
+  if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "batch: kernel does not fit on an SM");
+  if (O.ctas_per_sm > 0) bps = std::min(bps, O.ctas_per_sm);
+  *smem_out = smem;
+  *wpc_out = wpc;
+  *blocks_out = (int)std::min<int64_t>((int64_t)bps * h->num_sms, nunits);
+  return HC_OK;
+}
+
+static BatchLaunch batch_launch(hc_handle* h, const hc_options& O, const double* d_starts, int endgame,
+                                hc_path_result* d_results, double* d_solutions, const BatchUnit* units,
+                                int nunits) {
+  const int q = O.precision == HC_PREC_MIXED ? 1 : 0;
+  BatchLaunch bl{};
+  Launch& la = bl.base;
+  la.O = O;
+  la.npaths = h->btotal_paths;
+  la.starts = (const double2*)d_starts;
+  la.res = d_results;
+  la.sol = (double2*)d_solutions;
+  la.mode = endgame ? 1 : 0;
+  la.t1_re = 1.0;
+  la.t0_re = 0.0;
+  la.counter = h->d_counter;
+  la.cancel = h->d_cancel;
+  la.stats = h->d_counter + 1;
+  la.model = O.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+  la.phase = h->d_counter + 1 + HC_NSTATS;
+  bl.inst = h->d_binst[q];
+  bl.units = units;
+  bl.nunits = nunits;
+  bl.tbytes = h->btbytes[q];
+  bl.wstride = h->bwstride;
+  return bl;
 }
 
 int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_path_result* d_results,
@@ -902,22 +1067,11 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: null buffer");
   if (h->opts.step_control == HC_STEP_LEARNED && !h->d_model)
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: learned step control needs hc_set_step_model");
-  const int q = h->opts.precision == HC_PREC_MIXED ? 1 : 0;
-  const size_t smem_cap = 227 * 1024;
-  const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
-  int wpc = h->opts.warps_per_cta;
-  if (wpc <= 0) wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride));
-  size_t smem = fixed + (size_t)wpc * h->bwstride;
-  while (wpc > 1 && smem > smem_cap) {
-    --wpc;
-    smem = fixed + (size_t)wpc * h->bwstride;
-  }
-  if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "hc_track_batch_device: working set exceeds shared memory");
-  int bps = 0;
-  CK(prepare_batch(h->opts.precision, smem, wpc, &bps));
-  if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_batch_device: kernel does not fit on an SM");
-  if (h->opts.ctas_per_sm > 0) bps = std::min(bps, h->opts.ctas_per_sm);
-  int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, h->bnunits);
+  size_t smem = 0;
+  int wpc = 0, blocks = 0;
+  int rc = batch_geometry(h, h->opts, h->bnunits, &smem, &wpc, &blocks);
+  if (rc != HC_OK) return rc;
+  h->stats_on_host = false;
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
   const bool same = h->bgraph && h->bgraph_key[0] == d_starts && h->bgraph_key[1] == d_results &&
                     h->bgraph_key[2] == d_solutions && h->bgraph_endgame == (endgame ? 1 : 0) &&
@@ -925,26 +1079,7 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
   if (!same) {
     if (h->bgraph) cudaGraphExecDestroy(h->bgraph);
     h->bgraph = nullptr;
-    BatchLaunch bl{};
-    Launch& la = bl.base;
-    la.O = h->opts;
-    la.npaths = h->btotal_paths;
-    la.starts = (const double2*)d_starts;
-    la.res = d_results;
-    la.sol = (double2*)d_solutions;
-    la.mode = endgame ? 1 : 0;
-    la.t1_re = 1.0;
-    la.t0_re = 0.0;
-    la.counter = h->d_counter;
-    la.cancel = h->d_cancel;
-    la.stats = h->d_counter + 1;
-    la.model = h->opts.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
-    la.phase = h->d_counter + 1 + HC_NSTATS;
-    bl.inst = h->d_binst[q];
-    bl.units = h->d_bunits;
-    bl.nunits = h->bnunits;
-    bl.tbytes = h->btbytes[q];
-    bl.wstride = h->bwstride;
+    BatchLaunch bl = batch_launch(h, h->opts, d_starts, endgame, d_results, d_solutions, h->d_bunits, h->bnunits);
     // record: clear the queue head and counters, then the kernel
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -994,7 +1129,53 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
+  h->retracked = 0;
+  h->stats_on_host = true;
   if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
+  if (h->opts.step_control == HC_STEP_LEARNED && endgame) {
+    // per instance: re-track the paths whose endpoints coincide with plain step control, in place
+    std::vector<BatchUnit> units;
+    for (int i = 0; i < h->bninst; ++i) {
+      std::vector<int64_t> idx = coincident_paths(out_results + h->bpath_off[i],
+                                                  (const double2*)out_solutions + h->bvec_off[i], h->bnpaths[i],
+                                                  h->bn[i]);
+      for (int64_t k : idx) units.push_back(BatchUnit{i, (int)k, (int)k + 1, 0});
+    }
+    if (!units.empty()) {
+      if (h->runits_cap < units.size()) {
+        cudaFree(h->d_runits);
+        h->d_runits = nullptr;
+        h->runits_cap = 0;
+        CK(cudaMalloc(&h->d_runits, units.size() * sizeof(BatchUnit)));
+        h->runits_cap = units.size();
+      }
+      CK(cudaMemcpyAsync(h->d_runits, units.data(), units.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice,
+                         h->stream));
+      hc_options O = h->opts;
+      O.step_control = HC_STEP_PLAIN;
+      size_t smem = 0;
+      int wpc = 0, blocks = 0;
+      rc = batch_geometry(h, O, (int)units.size(), &smem, &wpc, &blocks);
+      if (rc != HC_OK) return rc;
+      BatchLaunch bl = batch_launch(h, O, (const double*)h->d_starts, endgame, h->d_res, (double*)h->d_sol,
+                                    h->d_runits, (int)units.size());
+      CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), h->stream));
+      CK(launch_batch(bl, blocks, wpc, smem, h->stream));
+      for (const BatchUnit& u : units) {
+        int64_t r = h->bpath_off[u.inst] + u.lo, e = h->bvec_off[u.inst] + (int64_t)u.lo * h->bn[u.inst];
+        CK(cudaMemcpyAsync(out_results + r, h->d_res + r, sizeof(hc_path_result), cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaMemcpyAsync(out_solutions + 2 * e, h->d_sol + e, h->bn[u.inst] * sizeof(double2),
+                           cudaMemcpyDeviceToHost, h->stream));
+      }
+      CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] += (double)st[i];
+      h->stats[0] -= (double)units.size();
+      h->retracked = (double)units.size();
+      if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
+    }
+  }
   return HC_OK;
 }
 
@@ -1012,7 +1193,7 @@ const char* hc_last_error(hc_handle* h) {
 
 int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
-  if (h->last_blocks > 0) {  // counters of the last call (hc_track or hc_track_device) on this handle
+  if (h->last_blocks > 0 && !h->stats_on_host) {  // counters of the last device-entry-point call
     unsigned long long st[HC_NSTATS + HC_NPHASE];
     CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->last_stream));
     CK(cudaStreamSynchronize(h->last_stream));
@@ -1024,8 +1205,9 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   // derived: [9] monomials M, [10] value terms, [11] Jacobian terms, [12] blocks, [13] warps
   // per block, [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree
   // monomial offset; [17] learned step proposals made, [18] of them rejected by Newton;
-  // [19 ..] cycle counters of the tracker phases (HcPhase order; profiling builds only)
-  double all[19 + HC_NPHASE];
+  // [19 ..] cycle counters of the tracker phases (HcPhase order; profiling builds only);
+  // [19 + HC_NPHASE] paths re-tracked with plain step control by the jump check
+  double all[20 + HC_NPHASE];
   for (int i = 0; i < 9; ++i) all[i] = h->stats[i];
   all[9] = h->prog.M;
   all[10] = (double)h->prog.val_terms;
@@ -1038,7 +1220,8 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   all[17] = h->stats[9];
   all[18] = h->stats[10];
   for (int k = 0; k < HC_NPHASE; ++k) all[19 + k] = h->stats[HC_NSTATS + k];
-  for (int i = 0; i < nout && i < 19 + HC_NPHASE; ++i) out[i] = all[i];
+  all[19 + HC_NPHASE] = h->retracked;
+  for (int i = 0; i < nout && i < 20 + HC_NPHASE; ++i) out[i] = all[i];
   return HC_OK;
 }
 

@@ -106,6 +106,7 @@ struct Launch {
   long long log_cap, log_lo, log_hi;
   const StepModel* model;  // learned step control (options.step_control == HC_STEP_LEARNED)
   unsigned long long* phase;  // [HC_NPHASE] phase cycle counters (profiling builds), may be null
+  const int64_t* path_list;   // if set: queue item i tracks path path_list[i] (in-place re-tracking)
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

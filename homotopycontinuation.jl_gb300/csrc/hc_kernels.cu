@@ -60,17 +60,18 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
     if (lane == 0) k = atomicAdd(la.counter, 1ULL);
     k = __shfl_sync(FULL, k, 0);
     if (k >= (unsigned long long)la.npaths) break;
+    const int64_t kk = la.path_list ? la.path_list[k] : (int64_t)k;
     if (T->cancelled()) {
       if (lane == 0) {
         hc_path_result R;
         memset(&R, 0, sizeof(R));
-        R.path_number = k + 1;
+        R.path_number = kk + 1;
         R.return_code = la.mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
-        la.res[k] = R;
+        la.res[kk] = R;
       }
       continue;
     }
-    T->run((int64_t)k);
+    T->run(kk);
     ++npaths_done;
   }
   __syncwarp();

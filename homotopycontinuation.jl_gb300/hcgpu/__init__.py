@@ -16,6 +16,7 @@ from .systems import (
     variables,
 )
 from .batch import BatchTracker, autotune_unit_paths, solve_batch
+from .parameters import FiniteException, ParameterHomotopy, ParametricSystem, parameter_homotopy
 from .tracking import (
     ENDGAME_CODES,
     TRACKER_CODES,

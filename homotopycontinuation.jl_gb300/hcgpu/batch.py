@@ -108,15 +108,18 @@ class BatchTracker:
                  sol[self.vec_off[i]:self.vec_off[i + 1]].reshape(-1, int(self.n[i])))
                 for i in range(len(self.homotopies))]
 
-    def solve(self, starts=None, seed=None):
-        res, sol = self.track_arrays(starts)
+    def solve(self, starts=None, seed=None, start_system="total_degree"):
+        """One Result per instance; ``starts`` as for track_arrays (default: total-degree)."""
+        flat = self.start_solutions() if starts is None else np.asarray(starts, dtype=np.complex128).reshape(-1)
+        res, sol = self.track_arrays(flat)
         out = []
         for i, (r, x) in enumerate(self.split(res, sol)):
             n = int(self.n[i])
             zv = np.zeros((r.shape[0], n))
             zl = np.zeros((r.shape[0], n), dtype=np.complex128)
-            prs = _path_results(r, x, zv, zl, None, self.options.endgame_start)
-            out.append(Result(prs, seed=seed, start_system="total_degree"))
+            Si = flat[self.vec_off[i]:self.vec_off[i + 1]].reshape(-1, n)
+            prs = _path_results(r, x, zv, zl, Si, self.options.endgame_start)
+            out.append(Result(prs, seed=seed, start_system=start_system))
         return out
 
     def stats(self):

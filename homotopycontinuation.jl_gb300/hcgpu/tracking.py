@@ -237,7 +237,7 @@ class _Handle:
                   "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"] + [
         "clk_" + p for p in ("run", "step", "predictor", "predict", "newton", "eval_jac", "eval", "taylor", "lu",
                              "solve", "norm", "stepsize", "endgame", "mono", "val_rows", "jac_rows", "refine",
-                             "init", "cond", "dd")]
+                             "init", "cond", "dd")] + ["paths_retracked"]
 
     def stats(self):
         out = np.zeros(len(self.STAT_NAMES))
@@ -312,6 +312,11 @@ class EndgameTracker:
         self._h.setup_step_control(self.tracker_options)
         self._h.set_homotopy(H)
 
+    def set_homotopy(self, H):
+        """Track another homotopy with the same options (e.g. new parameters)."""
+        self.homotopy = H
+        self._h.set_homotopy(H)
+
     def track_arrays(self, starts, t1: float = 1.0):
         return self._h.track(starts, endgame=True, t1=t1)
 
@@ -339,6 +344,10 @@ class Tracker:
         self.options = options or TrackerOptions()
         self._h = _Handle(make_options(self.options, None))
         self._h.setup_step_control(self.options)
+        self._h.set_homotopy(H)
+
+    def set_homotopy(self, H):
+        self.homotopy = H
         self._h.set_homotopy(H)
 
     def track_arrays(self, starts, t1=1.0, t0=0.0):
@@ -461,15 +470,31 @@ def nfailed(R: Result):
     return sum(1 for r in R.path_results if r.is_failed())
 
 
-def solve(F: System, start_system: str = "total_degree", gamma=None, seed=None, tracker_options=None,
-          endgame_options=None, precision: str = "fp64", step_control: str = "plain") -> Result:
+def solve(F, starts=None, start_system: str = "total_degree", *, start_parameters=None, target_parameters=None,
+          transform_result=None, transform_parameters=None, flatten: bool = False, gamma=None, seed=None,
+          tracker_options=None, endgame_options=None, precision: str = "fp64", step_control: str = "plain"):
     """solve(F; start_system = :total_degree) (src/solve.jl:447-526): one batched GPU call
-    replaces threaded_solve's per-path loop (src/solve.jl:628-709)."""
+    replaces threaded_solve's per-path loop (src/solve.jl:628-709).
+
+    With ``start_parameters`` (F a parameters.ParametricSystem, ``starts`` its solutions at the
+    start parameters): the parameter homotopy to ``target_parameters``; a list of target
+    parameter vectors runs the many-parameter solver in one launch (src/solve.jl:747-880)."""
+    if start_parameters is not None:
+        from . import parameters
+
+        if starts is None:
+            raise ValueError("a parameter homotopy needs start solutions")
+        return parameters.solve(F, starts, start_parameters, target_parameters, tracker_options=tracker_options,
+                                endgame_options=endgame_options, transform_result=transform_result,
+                                transform_parameters=transform_parameters, flatten=flatten,
+                                precision=precision, step_control=step_control)
     if start_system != "total_degree":
         raise NotImplementedError("only start_system='total_degree' is supported")
+    if starts is not None:
+        raise NotImplementedError("start solutions without start_parameters (a start system G) are not supported")
     to = tracker_options or TrackerOptions()
     to.precision = precision
     to.step_control = step_control
-    T, starts = total_degree(F, gamma=gamma, tracker_options=to, endgame_options=endgame_options, seed=seed)
-    prs = T.track_batch(starts)
+    T, S = total_degree(F, gamma=gamma, tracker_options=to, endgame_options=endgame_options, seed=seed)
+    prs = T.track_batch(S)
     return Result(prs, seed=seed, start_system=start_system)

@@ -109,7 +109,11 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
  * out_results[npaths], out_solutions[npaths×n complex]; out_valuation (npaths×n, may be NULL)
  * receives val_x (src/valuation.jl:6-22); out_last (npaths×n complex, may be NULL) receives
  * last_path_point with the endgame and val_tẋ (real parts) without it.
- * Copies in, runs and copies out on the handle's stream; returns when the results are on the host. */
+ * Copies in, runs and copies out on the handle's stream; returns when the results are on the host.
+ * With learned step control (and the endgame), paths whose nonsingular endpoints coincide with
+ * another path's — the mark of a path that jumped onto another path — are re-tracked in place
+ * with the plain step rule before returning (hc_last_stats [39] counts them); the device entry
+ * points return the tracker's results unchecked. */
 int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, double t1_re,
              double t1_im, double t0_re, double t0_im, hc_path_result* out_results,
              double* out_solutions, double* out_valuation, double* out_last);
@@ -137,7 +141,8 @@ const char* hc_last_error(hc_handle* h);
  * offset; [17] learned step proposals, [18] of them rejected by Newton; [19..38] cycles per
  * tracker phase (run, step, predictor, predict, newton, eval+Jacobian, eval, taylor, LU,
  * solve, norm, step size, endgame, monomials, value rows, Jacobian rows, refinement, init,
- * cond, double-double; inclusive), nonzero only in libraries built with -DHC_PHASE_CLOCKS.
+ * cond, double-double; inclusive), nonzero only in libraries built with -DHC_PHASE_CLOCKS;
+ * [39] paths re-tracked with plain step control by the jump check of hc_track/hc_track_batch.
  * No counterpart in the reference (its closest analogue is the Jacobian's factorization and
  * ldiv counters, src/linear_algebra.jl:809-862). */
 int hc_last_stats(hc_handle* h, double* out, int nout);
@@ -224,7 +229,8 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* instances
  * CUDA graph the first time a set of buffers is used and replayed afterwards. */
 int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame,
                           hc_path_result* d_results, double* d_solutions, void* stream);
-/* Same with host arrays; blocks until the results are in `out_results`/`out_solutions`. */
+/* Same with host arrays; blocks until the results are in `out_results`/`out_solutions`. With
+ * learned step control, applies hc_track's jump check within every instance. */
 int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_result* out_results,
                    double* out_solutions);
 

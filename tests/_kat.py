@@ -26,3 +26,12 @@ def winding_family(d):
     f1 = (a[0] * x**d + a[1] * y) * (a[2] * x + a[3] * y) + 1
     f2 = (a[0] * x**d + a[1] * y) * (a[4] * x + a[5] * y) + 1
     return hc.System.from_polys([f1, f2])
+
+
+def parametric_system(d):
+    """ParametricSystem from a term table over unknowns + parameters (fixtures' format)."""
+    nv, npar = d["nvars"], d["nparams"]
+    polys = []
+    for eq in d["equations"]:
+        polys.append(hc.Poly(nv + npar, {tuple(e): complex(*c) for e, c in zip(eq["exponents"], eq["coefficients"])}))
+    return hc.ParametricSystem.from_polys(polys, nv, npar)

@@ -40,6 +40,21 @@ def to_system(exprs, names):
             "coefficients": [[[c.real, c.imag] for c in cs] for cs in S.coefficients]}
 
 
+def to_param_system(exprs, names, params):
+    """Polynomials in the unknowns `names` and parameters `params` as one term table over
+    names + params (the test builds a ParametricSystem from it)."""
+    allv = list(names) + list(params)
+    vs = variables(len(allv))
+    env = dict(zip(allv, vs))
+    polys = [eval(julia_to_python(e), {}, env) for e in exprs]
+    eqs = []
+    for p in polys:
+        ks = sorted(p.terms)
+        eqs.append({"exponents": [list(k) for k in ks],
+                    "coefficients": [[p.terms[k].real, p.terms[k].imag] for k in ks]})
+    return {"nvars": len(names), "nparams": len(params), "equations": eqs}
+
+
 def split_top_level(s: str):
     out, depth, cur = [], 0, ""
     for ch in s:
@@ -62,7 +77,8 @@ def main(ref):
     eg = open(os.path.join(test, "endgame_tracker_test.jl")).read()
     en = open(os.path.join(test, "endgame_test.jl")).read()
     val = open(os.path.join(test, "valuation_test.jl")).read()
-    out = {"source": "HomotopyContinuation.jl test/endgame_tracker_test.jl, test/endgame_test.jl, test/valuation_test.jl"}
+    out = {"source": "HomotopyContinuation.jl test/endgame_tracker_test.jl, test/endgame_test.jl, "
+                     "test/valuation_test.jl, test/tracker_test.jl, test/solve_test.jl"}
 
     # EndgameTracker test: 2×2 quadrics, γ = 1.3im + 0.4
     m = re.search(r"f = \[(2\.3 \* x\^2.*?)\]\n\s*tracker, starts = total_degree\(System\(f\); gamma = ([^)]*)\)", eg)
@@ -87,6 +103,29 @@ def main(ref):
     # valuation example 3 (endgame side) system and targets
     m = re.search(r'Example 3.*?a = \[([^\]]*)\]', val, re.S)
     out["valuation_example3_a"] = [float(v) for v in m.group(1).split(",")]
+    # parameter homotopy (test/tracker_test.jl: Tracker(ParameterHomotopy(F, [1, 0], [2, 4])))
+    tr = open(os.path.join(test, "tracker_test.jl")).read()
+    m = re.search(r"F = System\(\[(x\^2 - a, x \* y - a \+ b)\], \[x, y\], \[a, b\]\)", tr)
+    h = re.search(r"ParameterHomotopy\(mode\(F\), \[([^\]]*)\], \[([^\]]*)\]\)", tr)
+    st = re.search(r"s = \[([^\]]*)\]\n\s*res = track\(tracker, s, 1, 0\)", tr)
+    steps = re.search(r"@test steps\(res\) ≤ (\d+)", tr)
+    sol = re.search(r"@test solution\(res\) ≈ \[sqrt\((\d+)\), -sqrt\((\d+)\)\]", tr)
+    out["parameter_tracker"] = {
+        **to_param_system(split_top_level(m.group(1)), ["x", "y"], ["a", "b"]),
+        "start_parameters": [float(v) for v in h.group(1).split(",")],
+        "target_parameters": [float(v) for v in h.group(2).split(",")],
+        "start": [float(v) for v in st.group(1).split(",")],
+        "expect": {"max_steps": int(steps.group(1)),
+                   "solution": [float(sol.group(1)) ** 0.5, -float(sol.group(2)) ** 0.5]}}
+    # solve (parameter homotopy): nsolutions == 1 (test/solve_test.jl)
+    sv = open(os.path.join(test, "solve_test.jl")).read()
+    blk = sv[sv.index('@testset "solve (parameter homotopy)"'):]
+    n1 = re.search(r"solve\(F, \[s\]; start_parameters = \[1, 0\], target_parameters = \[2, 4\]\)\n"
+                   r"\s*@test nsolutions\(res\) == (\d+)", blk)
+    fe = re.search(r"F = System\(\[(x\^2 - a)\], \[x, y\], \[a, b\]\)\n\s*s = \[1, 1\]\n\s*"
+                   r"@test_throws FiniteException\((\d+)\)", blk)
+    out["parameter_solve"] = {"expect": {"nsolutions": int(n1.group(1)), "finite_exception_dim": int(fe.group(2))},
+                              "underdetermined": to_param_system([fe.group(1)], ["x", "y"], ["a", "b"])}
     with open(os.path.join(HERE, "kat_systems.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(HERE, "kat_systems.json"))

@@ -106,3 +106,30 @@ def test_batch_rejects_bad_input():
     B = hc.BatchTracker([H])
     with pytest.raises(ValueError):
         B.track_arrays(np.zeros(3, dtype=np.complex128))
+
+
+def test_jump_check_with_learned_steps():
+    """Three instances of the 2,000-instance workload (seed 0) on which learned steps made a
+    path jump onto another path (two equal endpoints): the host entry points re-track the
+    coincident paths with plain steps, so every endpoint matches the plain FP64 tracker's."""
+    from hcgpu import learn
+
+    inst = hc.uneven_instances(2000, 0)
+    Hs = [hc.total_degree_homotopy(*inst[i]) for i in (278, 639, 1057)]
+    B64 = hc.BatchTracker(Hs, hc.TrackerOptions(precision="fp64"))
+    r64, x64 = B64.track_arrays()
+    for precision in ("fp64", "mixed"):
+        to = hc.TrackerOptions(precision=precision, step_control="learned", step_model=learn.default_model())
+        B = hc.BatchTracker(Hs, to)
+        r, x = B.track_arrays()
+        assert B.stats()["paths_retracked"] >= 2
+        assert (r["return_code"] == r64["return_code"]).all()
+        for (ri, xi), (r0, x0) in zip(B.split(r, x), B64.split(r64, x64)):
+            ok = (ri["return_code"] == 1) & (r0["return_code"] == 1)
+            assert rel_err(xi[ok], x0[ok]).max() <= 1e-10
+        # the single-homotopy host entry point applies the same check
+        T = hc.EndgameTracker(Hs[1], to)
+        rs, xs, _, _ = T.track_arrays(hc.total_degree_start_solutions(Hs[1].degrees))
+        assert T.stats()["paths_retracked"] >= 2
+        r0, x0 = B64.split(r64, x64)[1]
+        assert rel_err(xs, x0).max() <= 1e-10
