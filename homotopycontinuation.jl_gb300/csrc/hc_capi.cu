@@ -609,6 +609,15 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
                              double* d_solutions, double* d_valuation, double* d_last, cudaStream_t s,
                              const hc_options& O, const int64_t* d_path_list);
 
+// Warps per CTA when the options leave it open: as many as fit, except that mixed-precision
+// launches use 4 rather than 5..7 (one CTA per SM; with 5..7 warps some of the SM's four
+// schedulers run two warps and the others one, and the FP32-phase-heavy mixed tracker lost
+// 5% at 5 warps against 4 on 10 dense cubics, while the FP64 tracker gained 10%).
+static int balanced_warps(int wpc, int precision) {
+  if (precision == HC_PREC_MIXED && wpc > 4 && wpc < 8) return 4;
+  return wpc;
+}
+
 int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
                     double t1_im, double t0_re, double t0_im, hc_path_result* d_results, double* d_solutions,
                     double* d_valuation, double* d_last, void* stream) {
@@ -665,6 +674,7 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   if (wpc <= 0) {
     wpc = (int)std::min<size_t>(8, (smem_cap - la.T.bytes) / la.L.bytes);
     wpc = std::max(wpc, 1);
+    wpc = balanced_warps(wpc, O.precision);
   }
   size_t smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
   while (wpc > 1 && smem > smem_cap) {
@@ -1014,7 +1024,9 @@ static int batch_geometry(hc_handle* h, const hc_options& O, int nunits, size_t*
   const size_t smem_cap = 227 * 1024;
   const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
   int wpc = O.warps_per_cta;
-  if (wpc <= 0) wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride));
+  if (wpc <= 0)
+    wpc = balanced_warps((int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride)),
+                         O.precision);
   size_t smem = fixed + (size_t)wpc * h->bwstride;
   while (wpc > 1 && smem > smem_cap) {
     --wpc;
