@@ -17,6 +17,7 @@ from .systems import (
 )
 from .batch import BatchTracker, autotune_unit_paths, solve_batch
 from .io import read_parameters, read_solutions, write_parameters, write_solutions
+from .monodromy import MonodromyResult, find_start_pair, monodromy_solve
 from .parameters import FiniteException, ParameterHomotopy, ParametricSystem, parameter_homotopy
 from .tracking import (
     ENDGAME_CODES,

@@ -84,6 +84,20 @@ class ParametricSystem:
             Cs.append(np.array([acc[e][1] for e in ks], dtype=np.complex128).reshape(-1, nparams))
         return ParametricSystem(exps, c0s, Cs, nvars, nparams)
 
+    @staticmethod
+    def coefficient_parameters(F: System) -> "ParametricSystem":
+        """The family of all systems with F's support: every coefficient is a parameter (in
+        equation order); F itself is the member at parameters = its coefficients."""
+        total = sum(e.shape[0] for e in F.exponents)
+        C, off = [], 0
+        for e in F.exponents:
+            Ci = np.zeros((e.shape[0], total), dtype=np.complex128)
+            Ci[np.arange(e.shape[0]), off + np.arange(e.shape[0])] = 1.0
+            C.append(Ci)
+            off += e.shape[0]
+        return ParametricSystem([e.copy() for e in F.exponents], [np.zeros(e.shape[0]) for e in F.exponents], C,
+                                F.n, total)
+
     @property
     def n(self) -> int:
         return self.nvars
