@@ -18,6 +18,10 @@ namespace hcd {
 cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaStream_t stream);
 cudaError_t occupancy(int precision, int warps_per_cta, size_t smem, int* blocks_per_sm);
 cudaError_t prepare_batch(int precision, size_t smem, int warps_per_cta, int* blocks_per_sm);
+int certify_layout(const DevProg& P, int* bytes_out);
+cudaError_t launch_certify(const DevProg& P, int64_t nsols, const double* d_in, hc_certificate* d_out,
+                           double* d_centers, double* d_enclosures, int real_coefficients, int num_sms,
+                           cudaStream_t stream);
 cudaError_t launch_batch(const BatchLaunch& bl, int blocks, int warps_per_cta, size_t smem, cudaStream_t stream);
 }  // namespace hcd
 
@@ -1188,6 +1192,32 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
       if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
     }
   }
+  return HC_OK;
+}
+
+int hc_certify(hc_handle* h, int64_t ncand, const double* cand, int real_coefficients, hc_certificate* out,
+               double* out_centers, double* out_enclosures) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: null handle");
+  if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_certify: call hc_set_homotopy first");
+  if (ncand < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: ncandidates < 0");
+  if (ncand == 0) return HC_OK;
+  if (!cand || !out || !out_centers || !out_enclosures) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: null buffer");
+  int bytes = 0;
+  if (certify_layout(h->dprog, &bytes) != 0)
+    return fail(h, HC_ERR_TOO_LARGE, "hc_certify: the system's certification working set exceeds shared memory");
+  int n = h->prog.n;
+  int rc = ensure_capacity(h, ncand, n);
+  if (rc != HC_OK) return rc;
+  size_t nv = (size_t)ncand * n;
+  static_assert(sizeof(hc_certificate) <= sizeof(hc_path_result), "certificates reuse the result buffer");
+  hc_certificate* d_cert = (hc_certificate*)h->d_res;
+  CK(cudaMemcpyAsync(h->d_starts, cand, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  CK(launch_certify(h->dprog, ncand, (const double*)h->d_starts, d_cert, (double*)h->d_sol, (double*)h->d_last,
+                    real_coefficients ? 1 : 0, h->num_sms, h->stream));
+  CK(cudaMemcpyAsync(out, d_cert, (size_t)ncand * sizeof(hc_certificate), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(out_centers, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(out_enclosures, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return HC_OK;
 }
 

@@ -234,6 +234,21 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame,
 int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_result* out_results,
                    double* out_solutions);
 
+/* ---- Certification -------------------------------------------------------------------
+ * certify(F, solutions) (src/certification.jl:691-745): Krawczyk certificates for approximate
+ * solutions of F, the target system of the handle's homotopy (H at t = 0). Per candidate:
+ * certified = 1 if the polydisc B(center, radius) provably holds exactly one solution, which lies
+ * in the polydisc B(enclosure center, enclosure); realness = 1 if that solution is provably real
+ * (requires real_coefficients != 0, i.e. F has real coefficients), 2 if provably non-real, 0 if
+ * undecided. center is the candidate after one Newton step. Ball arithmetic in FP64 with upward
+ * rounded radii; one warp per candidate. */
+typedef struct hc_certificate {
+  int32_t certified, realness;
+  double radius, enclosure;
+} hc_certificate;
+int hc_certify(hc_handle* h, int64_t ncandidates, const double* candidates, int real_coefficients,
+               hc_certificate* out, double* out_centers, double* out_enclosure_centers);
+
 /* FP64 and FP32 CUDA-core FMA throughput of the current GPU in TFLOP/s, measured by a
  * short microbenchmark: the roofline denominators of this FP-pipe-bound path. No
  * counterpart in the reference. */

@@ -35,3 +35,21 @@ def parametric_system(d):
     for eq in d["equations"]:
         polys.append(hc.Poly(nv + npar, {tuple(e): complex(*c) for e, c in zip(eq["exponents"], eq["coefficients"])}))
     return hc.ParametricSystem.from_polys(polys, nv, npar)
+
+
+def term_lists(S):
+    """Per equation [(exponent tuple, complex coefficient)] of a System."""
+    return [[(tuple(int(v) for v in e), complex(c)) for e, c in zip(E, Cs)] for E, Cs in zip(S.exponents, S.coefficients)]
+
+
+def jacobian(S, x):
+    n = S.n
+    J = np.zeros((n, n), dtype=np.complex128)
+    for i, (E, Cs) in enumerate(zip(S.exponents, S.coefficients)):
+        for e, c in zip(E, Cs):
+            for j in range(n):
+                if e[j] > 0:
+                    d = e.copy()
+                    d[j] -= 1
+                    J[i, j] += c * e[j] * np.prod(x ** d)
+    return J

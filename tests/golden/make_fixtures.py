@@ -78,7 +78,8 @@ def main(ref):
     en = open(os.path.join(test, "endgame_test.jl")).read()
     val = open(os.path.join(test, "valuation_test.jl")).read()
     out = {"source": "HomotopyContinuation.jl test/endgame_tracker_test.jl, test/endgame_test.jl, "
-                     "test/valuation_test.jl, test/tracker_test.jl, test/solve_test.jl"}
+                     "test/valuation_test.jl, test/tracker_test.jl, test/solve_test.jl, "
+                     "test/certification_test.jl"}
 
     # EndgameTracker test: 2×2 quadrics, γ = 1.3im + 0.4
     m = re.search(r"f = \[(2\.3 \* x\^2.*?)\]\n\s*tracker, starts = total_degree\(System\(f\); gamma = ([^)]*)\)", eg)
@@ -126,6 +127,25 @@ def main(ref):
                    r"@test_throws FiniteException\((\d+)\)", blk)
     out["parameter_solve"] = {"expect": {"nsolutions": int(n1.group(1)), "finite_exception_dim": int(fe.group(2))},
                               "underdetermined": to_param_system([fe.group(1)], ["x", "y"], ["a", "b"])}
+    # certification (test/certification_test.jl "Simple 1")
+    ce = open(os.path.join(test, "certification_test.jl")).read()
+    blk = ce[ce.index('@testset "Simple 1'):]
+    f1 = re.search(r"f₁ = (.*)\n", blk).group(1).strip()
+    f2 = re.search(r"f₂ = (.*)\n", blk).group(1).strip()
+    num = lambda pat: int(re.search(pat, blk).group(1))
+    d2 = blk[blk.index("# Double solutions"):]
+    num2 = lambda pat: int(re.search(pat, d2).group(1))
+    out["certification_simple"] = {
+        **to_system([f1, f2], ["x", "y"]),
+        "expect": {"nnonsingular": num(r"@test nnonsingular\(result\) == (\d+)"),
+                   "ncertified": num(r"@test ncertified\(cert\) == (\d+)"),
+                   "ndistinct_certified": num(r"@test ndistinct_certified\(cert\) == (\d+)"),
+                   "nreal_certified": num(r"@test nreal_certified\(cert\) == (\d+)"),
+                   "ncomplex_certified": num(r"@test ncomplex_certified\(cert\) == (\d+)"),
+                   "doubled": {"ncertified": num2(r"@test ncertified\(cert\) == (\d+)"),
+                               "ndistinct_certified": num2(r"@test ndistinct_certified\(cert\) == (\d+)"),
+                               "nreal_certified": num2(r"@test nreal_certified\(cert\) == (\d+)"),
+                               "ndistinct_real_certified": num2(r"@test ndistinct_real_certified\(cert\) == (\d+)")}}}
     with open(os.path.join(HERE, "kat_systems.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(HERE, "kat_systems.json"))
