@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--paths", type=int, default=0, help="track only the first N paths (profiling cases)")
+    p.add_argument("--autotune", action="store_true",
+                   help="uneven workload: tune the paths per CTA work unit for every n first")
     p.add_argument("--workload", default="dense", choices=list(WORKLOADS),
                    help="dense: the headline workload; sparse and uneven: the endgame-heavy and batched cases")
     return p.parse_args()
@@ -387,8 +389,18 @@ def main_uneven(args, torch, hc, _lib, local):
     torch.cuda.set_stream(stream)
     L = _lib.load()
 
+    unit_paths = None
+    tune_s = 0.0
+    if args.autotune:
+        t = time.perf_counter()
+        unit_paths = hc.autotune_unit_paths(Hs, hc.TrackerOptions(precision=args.precision,
+                                                                   step_control=args.step_control),
+                                            candidates=(2, 4, 8, 16, 32), sample=60)
+        tune_s = time.perf_counter() - t
+
     def batch(precision, step_control):
-        return hc.BatchTracker(Hs, hc.TrackerOptions(precision=precision, step_control=step_control))
+        return hc.BatchTracker(Hs, hc.TrackerOptions(precision=precision, step_control=step_control),
+                               unit_paths=unit_paths)
 
     B = batch(args.precision, args.step_control)
     S = B.start_solutions()
@@ -469,6 +481,9 @@ def main_uneven(args, torch, hc, _lib, local):
             "config": {"workload": WORKLOADS["uneven"], "seed": args.seed, "instances": len(Hs),
                        "paths": B.total_paths, "precision": args.precision, "step_control": args.step_control,
                        "ctas": stats["blocks"], "warps_per_cta": stats["warps_per_block"],
+                       "unit_paths": ({str(k): int(v) for k, v in unit_paths.items()} if unit_paths
+                                      else "default: one path per warp of a CTA"),
+                       "autotune_seconds": tune_s,
                        "l2": "256 MiB buffer written between timed steps"},
             "e2e": {"value": B.total_paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(S.nbytes),
                     "d2h_bytes_per_step": int(out_res.nbytes + out_sol.nbytes)},

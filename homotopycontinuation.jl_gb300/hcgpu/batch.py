@@ -136,7 +136,7 @@ def solve_batch(instances, tracker_options=None, endgame_options=None, unit_path
     return BatchTracker(Hs, tracker_options, endgame_options, unit_paths=unit_paths).solve()
 
 
-def autotune_unit_paths(homotopies, tracker_options=None, candidates=(8, 16, 32, 64, 128), sample=None,
+def autotune_unit_paths(homotopies, tracker_options=None, candidates=(2, 4, 8, 16, 32, 64), sample=None,
                         repeats=1, verbose=False):
     """Choose the paths per CTA work unit for every n in the batch: for each n, the batch of
     that n's instances (or ``sample`` of them) is tracked with each candidate unit size and the

@@ -219,7 +219,7 @@ typedef struct hc_instance_desc {
 
 /* Compile and upload a batch (replacing any previous batch of the handle). The kernel's CTAs
  * take work units of at most unit_paths[n] paths of one instance with n variables
- * (unit_paths: 33 entries indexed by n, NULL or 0 = 4 paths per warp of a CTA); units are
+ * (unit_paths: 33 entries indexed by n, NULL or 0 = one path per warp of a CTA); units are
  * queued largest estimated cost first. `total_paths` and `total_elements` (optional) receive
  * Σ npaths_i and Σ npaths_i·n_i. */
 int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* instances,
