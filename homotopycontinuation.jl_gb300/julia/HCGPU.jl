@@ -232,4 +232,42 @@ function gpu_solve_many(Fs::Vector{<:HC.System}; gammas = [cis(2π * rand()) for
     end
 end
 
+struct HCCertificate  # hc_certificate
+    certified::Int32
+    realness::Int32
+    radius::Float64
+    enclosure::Float64
+end
+
+"""
+    gpu_certify(F::System, solutions)
+
+Krawczyk certificates for approximate solutions of `F` (hc_certify): returns the vector of
+`HCCertificate` records (certified, realness 1 = real / 2 = non-real / 0 = undecided, box
+radius, enclosure radius), the refined box centres and the enclosure centres.
+"""
+function gpu_certify(F::HC.System, solutions::AbstractVector{<:AbstractVector})
+    T = homotopy_tables(F)
+    n, m = T.n, length(solutions)
+    S = Vector{Float64}(undef, 2n * m)
+    for (k, s) in enumerate(solutions), i in 1:n
+        S[2(n*(k-1)+i)-1] = real(s[i]); S[2(n*(k-1)+i)] = imag(s[i])
+    end
+    realcoef = all(c -> imag(c) == 0, T.Fcf[2:2:end]) ? 1 : 0
+    with_handle(0) do h
+        check(ccall((:hc_set_homotopy, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Int32},
+                     Ptr{Int32}, Ptr{Float64}, Float64, Float64),
+                    h, n, length(T.Geq), T.Geq, T.Gexp, T.Gcf, length(T.Feq), T.Feq, T.Fexp, T.Fcf,
+                    1.0, 0.0), h)
+        certs = Vector{HCCertificate}(undef, m)
+        centers = Vector{Float64}(undef, 2n * m)
+        encl = Vector{Float64}(undef, 2n * m)
+        check(ccall((:hc_certify, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Int64, Ptr{Float64}, Cint, Ptr{HCCertificate}, Ptr{Float64}, Ptr{Float64}),
+                    h, m, S, realcoef, certs, centers, encl), h)
+        (certs, centers, encl)
+    end
+end
+
 end # module
