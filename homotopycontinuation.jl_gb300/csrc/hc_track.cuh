@@ -768,20 +768,30 @@ struct PathTracker {
       int kp = k;
       R amax = vk;
       if (!isnan(vk)) {
-        R bv = (LANE > k && LANE < n && !isnan(v)) ? v : (R)-1;
-        if (LANE == k) bv = vk;
-        int bi = (LANE >= k && LANE < n) ? LANE : 1 << 30;
+        if constexpr (std::is_same<R, float>::value) {
+          // non-negative FP32 magnitudes order like their bit patterns: one warp max-reduction
+          // and the lowest candidate lane holding it (the same maximum and tie rule as below)
+          const bool cand = LANE >= k && LANE < n && (LANE == k || !isnan(v));
+          const unsigned key = cand ? __float_as_uint(v) : 0u;
+          const unsigned mx = __reduce_max_sync(FULL, key);
+          kp = __ffs(__ballot_sync(FULL, cand && key == mx)) - 1;
+          amax = __uint_as_float(mx);
+        } else {
+          R bv = (LANE > k && LANE < n && !isnan(v)) ? v : (R)-1;
+          if (LANE == k) bv = vk;
+          int bi = (LANE >= k && LANE < n) ? LANE : 1 << 30;
 #pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          R ov = __shfl_xor_sync(FULL, bv, o);
-          int oi = __shfl_xor_sync(FULL, bi, o);
-          if (ov > bv || (ov == bv && oi < bi)) {
-            bv = ov;
-            bi = oi;
+          for (int o = 16; o; o >>= 1) {
+            R ov = __shfl_xor_sync(FULL, bv, o);
+            int oi = __shfl_xor_sync(FULL, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) {
+              bv = ov;
+              bi = oi;
+            }
           }
+          kp = bi;
+          amax = bv;
         }
-        kp = bi;
-        amax = bv;
       }
       if (LANE == 0) ipiv[k] = kp;
       if (amax != (R)0) {
@@ -812,11 +822,10 @@ struct PathTracker {
         }
         __syncwarp();
       }
-      int m = n - k - 1;
-      int tot = m * m;
-      for (int e = LANE; e < tot; e += 32) {
-        int i = k + 1 + e % m, j = k + 1 + e / m;
-        A[j * n + i] = cfms(A[k * n + i], A[j * n + k], A[j * n + i]);
+      // trailing update, lane i over the rows below the pivot (column after column)
+      if (LANE > k && LANE < n) {
+        const T l = A[k * n + LANE];
+        for (int j = k + 1; j < n; ++j) A[j * n + LANE] = cfms(l, A[j * n + k], A[j * n + LANE]);
       }
       __syncwarp();
     }
