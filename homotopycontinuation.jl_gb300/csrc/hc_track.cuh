@@ -618,18 +618,20 @@ struct PathTracker {
           }
         }
         const T* Sp = S + d.x * 4;
+        // a parent's orders up to hi feed its children; a top-degree monomial needs lo and hi only
+        const bool parent = m < top;
         T c[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           T acc;
           acc.re = acc.im = 0;
-          if (k <= K) {
+          if (parent ? k <= hi : (k == lo || k == hi)) {
 #pragma unroll
             for (int j = 0; j <= k; ++j) acc = cfma(Sp[j], X[k - j], acc);
           }
           c[k] = acc;
         }
-        if (m < top) {
+        if (parent) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) S[m * 4 + k] = c[k];
         } else {
@@ -761,6 +763,9 @@ struct PathTracker {
     // pivots are those of an FP64 search on the same values, without FP64 instructions
     using R = decltype(T{}.re);
     T* dv = (T*)dinv;  // reciprocal pivots in T
+    // the row interchanges composed into one permutation: lane i ends with the source row of
+    // row i (stored with its inverse, so that each solve permutes with one shuffle)
+    int perm = LANE;
     for (int k = 0; k < n; ++k) {
       R v = -1;
       if (LANE >= k && LANE < n) v = abs2(A[k * n + LANE]);
@@ -793,7 +798,11 @@ struct PathTracker {
           amax = bv;
         }
       }
-      if (LANE == 0) ipiv[k] = kp;
+      if (kp != k) {
+        const int pk = __shfl_sync(FULL, perm, k), pp = __shfl_sync(FULL, perm, kp);
+        if (LANE == k) perm = pp;
+        if (LANE == kp) perm = pk;
+      }
       if (amax != (R)0) {
         if (kp != k) {
           if (LANE < n) {
@@ -829,6 +838,12 @@ struct PathTracker {
       }
       __syncwarp();
     }
+    unsigned char* pv = (unsigned char*)ipiv;
+    if (LANE < n) {
+      pv[LANE] = (unsigned char)perm;
+      pv[32 + perm] = (unsigned char)LANE;
+    }
+    __syncwarp();
   }
   __device__ HC_NI void factorize() {
     HC_PHASE(PH_LU);
@@ -843,15 +858,7 @@ struct PathTracker {
   template <class T>
   __device__ HC_NI c64 lu_solve_T(c64 b64) {
     const T* A = (const T*)LUb;
-    T b = conv<T>(b64);
-    for (int i = 0; i < n; ++i) {
-      int p = ipiv[i];
-      if (p != i) {
-        T vi = shfl(b, i), vp = shfl(b, p);
-        if (LANE == i) b = vp;
-        if (LANE == p) b = vi;
-      }
-    }
+    T b = shfl(conv<T>(b64), LANE < n ? (int)((const unsigned char*)ipiv)[LANE] : LANE);
     const T* dv = (const T*)dinv;
     for (int j = 0; j < n; ++j) {
       T xj = shfl(b, j);
@@ -880,14 +887,7 @@ struct PathTracker {
       T xi = shfl(b, i);
       if (LANE < i) b = b - conj(A[LANE * n + i]) * xi;
     }
-    for (int i = n - 1; i >= 0; --i) {  // _inverse_ipiv!
-      int p = ipiv[i];
-      if (p != i) {
-        T vi = shfl(b, i), vp = shfl(b, p);
-        if (LANE == i) b = vp;
-        if (LANE == p) b = vi;
-      }
-    }
+    b = shfl(b, LANE < n ? (int)((const unsigned char*)ipiv)[32 + LANE] : LANE);  // _inverse_ipiv!
     ++c_solve;
     return LANE < n ? to64(b) : C64(0.0);
   }
