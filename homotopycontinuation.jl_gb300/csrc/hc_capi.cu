@@ -55,6 +55,7 @@ struct HostProg {
   std::vector<float2> vcoef32;
   std::vector<uint16_t> vmono;
   std::vector<uint32_t> jcode;
+  std::vector<int> vorig;  // value term k of the program is the caller's term vorig[k] (F, then G)
   // operation census for the flop model
   long long val_terms = 0, jac_terms = 0;
 };
@@ -140,9 +141,11 @@ void build_segments(int nrows, const std::vector<Term>& terms, int per_lane, Hos
   }
 }
 
+// full_series: every monomial keeps four Taylor orders (the toric homotopy's series rows read
+// all of them), not only the two the straight-line rows need of the top degree
 int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const double* G_coef, int nF,
                   const int32_t* F_eq, const int32_t* F_exps, const double* F_coef, HostProg& P,
-                  std::string& err) {
+                  std::string& err, bool full_series = false) {
   MonoTable mt(n);
   std::vector<int> zero(n, 0);
   mt.insert(zero);
@@ -209,7 +212,7 @@ int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, con
     P.lev[maxdeg + 1] = cur;
   }
   P.nlev = maxdeg + 1;
-  P.top = P.lev[maxdeg];
+  P.top = full_series ? P.M : P.lev[maxdeg];
   // value terms (rows F_0..F_{n-1}, G_0..G_{n-1}) in caller order, then stably sorted by row
   std::vector<Term> vt;
   std::vector<std::vector<int>> vexp;
@@ -226,7 +229,9 @@ int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, con
   P.vcoef64.resize(vt.size());
   P.vcoef32.resize(vt.size());
   P.vmono.resize(vt.size());
+  P.vorig.resize(vt.size());
   for (size_t k = 0; k < vt.size(); ++k) {
+    P.vorig[k] = vt[k].orig;
     P.vcoef64[k] = make_double2(vt[k].re, vt[k].im);
     P.vcoef32[k] = make_float2((float)vt[k].re, (float)vt[k].im);
     P.vmono[k] = (uint16_t)vt[k].mono;
@@ -280,7 +285,7 @@ TableLayout make_table_layout(const HostProg& P, int precision) {
   return T;
 }
 
-WarpLayout make_warp_layout(const HostProg& P) {
+WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0) {
   WarpLayout L{};
   int n = P.n;
   int vn = (n + 1) & ~1;
@@ -303,6 +308,8 @@ WarpLayout make_warp_layout(const HostProg& P) {
   L.vec = take((size_t)HC_NCVEC * vn * 16);
   L.rvec = take((size_t)HC_NRVEC * vn * 8);
   L.v32 = take((size_t)4 * vn * 8);
+  L.tor = tor_n > 0 ? take((size_t)tor_n * (16 + 8 + 8)) : 0;
+  L.tor_n = tor_n;
   L.vn = vn;
   L.bytes = (int)off;
   return L;
@@ -418,6 +425,13 @@ struct hc_handle {
   bool stats_on_host = false;  // the last call was a host entry point: its counters are final
   int last_blocks = 0, last_wpc = 0;
   cudaStream_t last_stream = nullptr;
+  // toric homotopy (hc_set_toric): weight rows in program term order, per-path arguments
+  bool toric = false;
+  int tor_rows = 0;
+  double* d_tor_w = nullptr;
+  size_t tor_w_cap = 0;
+  char* d_tor_path = nullptr;  // [4 × npaths doubles: t1, t0, ω, μ][npaths int32 rows]
+  size_t tor_path_cap = 0;
   // step log
   double* d_log = nullptr;
   unsigned long long* d_log_count = nullptr;
@@ -524,6 +538,8 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_bunits);
   cudaFree(h->d_plist);
   cudaFree(h->d_runits);
+  cudaFree(h->d_tor_w);
+  cudaFree(h->d_tor_path);
   if (h->bgraph) cudaGraphExecDestroy(h->bgraph);
   cudaFree(h->d_log);
   cudaFree(h->d_log_count);
@@ -577,6 +593,7 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   h->dprog = D;
   h->layout = L;
   h->has_prog = true;
+  h->toric = false;
   return HC_OK;
 }
 
@@ -608,10 +625,16 @@ static int ensure_capacity_v(hc_handle* h, int64_t npaths, int64_t nvec) {
 }
 static int ensure_capacity(hc_handle* h, int64_t npaths, int n) { return ensure_capacity_v(h, npaths, npaths * n); }
 
+// per-path overrides and the toric weights of a plain-tracker launch (all optional)
+struct PathArgs {
+  const double *t1 = nullptr, *t0 = nullptr, *omega = nullptr, *mu = nullptr;
+  const double* tor_w = nullptr;
+  const int32_t* tor_row = nullptr;
+};
 static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
                              double t1_im, double t0_re, double t0_im, hc_path_result* d_results,
                              double* d_solutions, double* d_valuation, double* d_last, cudaStream_t s,
-                             const hc_options& O, const int64_t* d_path_list);
+                             const hc_options& O, const int64_t* d_path_list, const PathArgs& pa = PathArgs());
 
 // Warps per CTA when the options leave it open: as many as fit, except that mixed-precision
 // launches use 4 rather than 5..7 (one CTA per SM; with 5..7 warps some of the SM's four
@@ -627,6 +650,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
                     double* d_valuation, double* d_last, void* stream) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null handle");
   if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_device: call hc_set_homotopy first");
+  if (h->toric) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: the handle holds a toric homotopy (hc_track_toric)");
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: npaths < 0");
   if (npaths == 0) return HC_OK;
   if (!d_starts || !d_results || !d_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null buffer");
@@ -643,7 +667,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
 static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_starts, int endgame, double t1_re,
                              double t1_im, double t0_re, double t0_im, hc_path_result* d_results,
                              double* d_solutions, double* d_valuation, double* d_last, cudaStream_t s,
-                             const hc_options& O, const int64_t* d_path_list) {
+                             const hc_options& O, const int64_t* d_path_list, const PathArgs& pa) {
   Launch la{};
   la.P = h->dprog;
   la.O = O;
@@ -671,6 +695,12 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   la.model = O.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
   la.phase = h->d_counter + 1 + HC_NSTATS;
   la.path_list = d_path_list;
+  la.path_t1 = pa.t1;
+  la.path_t0 = pa.t0;
+  la.path_omega = pa.omega;
+  la.path_mu = pa.mu;
+  la.tor_w = pa.tor_w;
+  la.tor_row = pa.tor_row;
   if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
   // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
   const size_t smem_cap = 227 * 1024;
@@ -740,6 +770,7 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
              double* out_last) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track: null handle");
   if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track: call hc_set_homotopy first");
+  if (h->toric) return fail(h, HC_ERR_INVALID_ARG, "hc_track: the handle holds a toric homotopy (hc_track_toric)");
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track: npaths < 0");
   if (npaths == 0) return HC_OK;
   if (!starts || !out_results || !out_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track: null buffer");
@@ -845,6 +876,120 @@ static uint16_t to_bf16(float f) {  // round to nearest even; NaN stays NaN
   if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);
   u += 0x7fffu + ((u >> 16) & 1u);
   return (uint16_t)(u >> 16);
+}
+
+int hc_set_toric(hc_handle* h, int n, int nF, const int32_t* F_eq, const int32_t* F_exps, const double* F_coef,
+                 int nrows, const double* weights) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: null handle");
+  if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_set_toric: need 1 <= n <= 32");
+  if (nF < 1 || !F_eq || !F_exps || !F_coef) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: bad term table");
+  if (nrows < 1 || !weights) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: need at least one weight row");
+  for (size_t k = 0; k < (size_t)nrows * nF; ++k)
+    if (!(weights[k] >= 0.0) || !std::isfinite(weights[k]))
+      return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: weights must be finite and non-negative");
+  HostProg P;
+  std::string err;
+  int rc = build_program(n, 0, nullptr, nullptr, nullptr, nF, F_eq, F_exps, F_coef, P, err, true);
+  if (rc != HC_OK) return fail(h, rc, "hc_set_toric: " + err);
+  const int T = (int)P.vcoef64.size();
+  WarpLayout L = make_warp_layout(P, T);
+  TableLayout TL = make_table_layout(P, HC_PREC_FP64);
+  if ((size_t)TL.bytes + L.bytes > 220 * 1024)
+    return fail(h, HC_ERR_TOO_LARGE, "hc_set_toric: tables plus one path's working set exceed shared memory");
+  // weight rows in program term order
+  std::vector<double> w((size_t)nrows * T);
+  for (int r = 0; r < nrows; ++r)
+    for (int k = 0; k < T; ++k) w[(size_t)r * T + k] = weights[(size_t)r * nF + P.vorig[k]];
+  std::vector<char> blob;
+  ProgOffsets po = pack_program(P, blob);
+  if (h->d_prog_bytes < blob.size()) {
+    cudaFree(h->d_prog);
+    h->d_prog = nullptr;
+    h->d_prog_bytes = 0;
+    CK(cudaMalloc(&h->d_prog, blob.size()));
+    h->d_prog_bytes = blob.size();
+  }
+  if (h->tor_w_cap < w.size()) {
+    cudaFree(h->d_tor_w);
+    h->d_tor_w = nullptr;
+    h->tor_w_cap = 0;
+    CK(cudaMalloc(&h->d_tor_w, w.size() * sizeof(double)));
+    h->tor_w_cap = w.size();
+  }
+  CK(cudaMemcpyAsync(h->d_prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_tor_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  DevProg D = bind_program(P, po, h->d_prog, 1.0, 0.0);
+  h->prog = std::move(P);
+  h->dprog = D;
+  h->layout = L;
+  h->has_prog = true;
+  h->toric = true;
+  h->tor_rows = nrows;
+  return HC_OK;
+}
+
+int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int32_t* rows, const double* t1,
+                   const double* t0, const double* omega, const double* mu, hc_path_result* out_results,
+                   double* out_solutions) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: null handle");
+  if (!h->has_prog || !h->toric) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_toric: call hc_set_toric first");
+  if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: npaths < 0");
+  if (npaths == 0) return HC_OK;
+  if (!starts || !rows || !t1 || !t0 || !out_results || !out_solutions)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: null buffer");
+  for (int64_t k = 0; k < npaths; ++k) {
+    if (rows[k] < 0 || rows[k] >= h->tor_rows)
+      return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: weight row out of range");
+    if (!std::isfinite(t1[k]) || !std::isfinite(t0[k]) || t1[k] < 0.0 || t0[k] < 0.0)
+      return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: times must be finite and non-negative");
+  }
+  const int n = h->prog.n;
+  int rc = ensure_capacity(h, npaths, n);
+  if (rc != HC_OK) return rc;
+  const size_t nv = (size_t)npaths * n;
+  const size_t pbytes = (size_t)npaths * (4 * sizeof(double) + sizeof(int32_t));
+  if (h->tor_path_cap < pbytes) {
+    cudaFree(h->d_tor_path);
+    h->d_tor_path = nullptr;
+    h->tor_path_cap = 0;
+    CK(cudaMalloc(&h->d_tor_path, pbytes));
+    h->tor_path_cap = pbytes;
+  }
+  double* dp = (double*)h->d_tor_path;
+  int32_t* drow = (int32_t*)(dp + 4 * npaths);
+  PathArgs pa;
+  pa.t1 = dp;
+  pa.t0 = dp + npaths;
+  pa.omega = omega ? dp + 2 * npaths : nullptr;
+  pa.mu = mu ? dp + 3 * npaths : nullptr;
+  pa.tor_w = h->d_tor_w;
+  pa.tor_row = drow;
+  *h->h_cancel = 0;
+  CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dp, t1, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dp + npaths, t0, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (omega) CK(cudaMemcpyAsync(dp + 2 * npaths, omega, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (mu) CK(cudaMemcpyAsync(dp + 3 * npaths, mu, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(drow, rows, npaths * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  // the toric tracker runs in FP64 with the plain step rule
+  hc_options O = h->opts;
+  O.precision = HC_PREC_FP64;
+  O.step_control = HC_STEP_PLAIN;
+  rc = track_device_impl(h, npaths, (const double*)h->d_starts, 0, 0.0, 0.0, 1.0, 0.0, h->d_res, (double*)h->d_sol,
+                         nullptr, nullptr, h->stream, O, nullptr, pa);
+  if (rc != HC_OK) return rc;
+  CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)npaths * sizeof(hc_path_result), cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long st[HC_NSTATS + HC_NPHASE];
+  CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
+  h->retracked = 0;
+  h->stats_on_host = true;
+  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_toric: cancelled");
+  return HC_OK;
 }
 
 int hc_set_step_model(hc_handle* h, const float* params, const float* mean, const float* std, double confidence,

@@ -53,6 +53,8 @@ struct WarpLayout {
   int rvec;  // real vectors (vn elements each, 8 B)
   int vn;    // padded vector length (elements)
   int v32;   // FP32 staging: x (FP32 Jacobians) or tx0..tx2 (FP32 Taylor series), 4 × vn c32
+  int tor;   // toric homotopy: coefficients u·t^w (c64), t^w and w (double) of the current path
+  int tor_n; // value terms of the toric program (0: not a toric homotopy)
 };
 constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
 constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
@@ -107,6 +109,13 @@ struct Launch {
   const StepModel* model;  // learned step control (options.step_control == HC_STEP_LEARNED)
   unsigned long long* phase;  // [HC_NPHASE] phase cycle counters (profiling builds), may be null
   const int64_t* path_list;   // if set: queue item i tracks path path_list[i] (in-place re-tracking)
+  // per-path overrides of the plain tracker (mode 0), each null or [npaths]: start and target
+  // time (real), initial ω and μ (NaN: computed by init_newton)
+  const double *path_t1, *path_t0, *path_omega, *path_mu;
+  // toric homotopy of the polyhedral method: value-term weights, one row per mixed cell
+  // (program term order, tor_n per row), and the row of each path
+  const double* tor_w;
+  const int32_t* tor_row;
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

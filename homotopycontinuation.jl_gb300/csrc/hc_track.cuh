@@ -189,6 +189,14 @@ struct PathTracker {
   double pred_delta;  // relative correction of the last ẋ refinement step (≈ FP32 solve error)
   c64 tJ;     // t of the last Jacobian evaluation (its x is xJ)
 
+  // ---- ToricHomotopy (src/homotopies/toric_homotopy.jl:9-35): the current path's weights w
+  // and its coefficients u·t^w, cached for the t of the last evaluation (tc_t)
+  bool toric;
+  c64* tcoef;
+  double *tpow, *tw;
+  double tc_t;
+  const c64* vc;  // value-term coefficients the rows read: vcoef64, or tcoef
+
   // ---- Predictor state (src/predictor.jl:72-103)
   int pmethod, porder, wnum;
   double trust_region, local_error, cond_H_xd;
@@ -303,6 +311,12 @@ struct PathTracker {
     winv = rv + 19 * vn;
     dinv = (c64*)(base + L.dinv);
     v32 = (c32*)(base + L.v32);
+    toric = !MIXED && la->tor_w != nullptr && L.tor_n > 0;
+    tcoef = (c64*)(base + L.tor);
+    tpow = (double*)(tcoef + L.tor_n);
+    tw = tpow + L.tor_n;
+    tc_t = dNaN();
+    vc = toric ? (const c64*)tcoef : vcoef64;
     factorized = scaled = false;
     Aprec = 64;
     j64 = false;
@@ -444,13 +458,13 @@ struct PathTracker {
       int t = g.y;
       for (; t + 4 <= g.z; t += 4) {
         int m0 = vmono[t], m1 = vmono[t + 1], m2 = vmono[t + 2], m3 = vmono[t + 3];
-        c64 c0 = vcoef64[t], c1 = vcoef64[t + 1], c2 = vcoef64[t + 2], c3 = vcoef64[t + 3];
+        c64 c0 = vc[t], c1 = vc[t + 1], c2 = vc[t + 2], c3 = vc[t + 3];
         a0 = cfma(c0, mono64[m0], a0);
         a1 = cfma(c1, mono64[m1], a1);
         a2 = cfma(c2, mono64[m2], a2);
         a3 = cfma(c3, mono64[m3], a3);
       }
-      for (; t < g.z; ++t) a0 = cfma(vcoef64[t], mono64[vmono[t]], a0);
+      for (; t < g.z; ++t) a0 = cfma(vc[t], mono64[vmono[t]], a0);
       pp[g.w & 0xffffff] = (a0 + a1) + (a2 + a3);
     }
     __syncwarp();
@@ -472,7 +486,7 @@ struct PathTracker {
     const T* cf;
     if constexpr (std::is_same<T, c64>::value) {
       mv = mono64;
-      cf = vcoef64;
+      cf = vc;
     } else {
       mv = (const c32*)(mono64 + P->M);
       cf = vcoef32;
@@ -504,9 +518,13 @@ struct PathTracker {
     T* A = (T*)Ab;
     T ts = conv<T>(ts64), tt = conv<T>(tt64);
     int nn = n * n;
-    for (int e = LANE; e < nn; e += 32) {
-      T f = row_sum(R, pp, e), gg = row_sum(R, pp, nn + e);
-      A[e] = ts * gg + tt * f;
+    if (toric) {
+      for (int e = LANE; e < nn; e += 32) A[e] = row_sum(R, pp, e);
+    } else {
+      for (int e = LANE; e < nn; e += 32) {
+        T f = row_sum(R, pp, e), gg = row_sum(R, pp, nn + e);
+        A[e] = ts * gg + tt * f;
+      }
     }
     __syncwarp();
   }
@@ -514,23 +532,32 @@ struct PathTracker {
   // H(x,t) (src/homotopies/straight_line_homotopy.jl:96-104) → out (vector)
   __device__ HC_NI void H_eval(const c64* xv, c64 t, c64* out) {
     HC_PHASE(PH_EVAL);
+    if (toric) toric_coeffs(t.re);
     eval_mono64(xv);
     c64 F, G;
     val_rows64(F, G);
-    c64 ts = gamma() * t, tt = C64(1.0) - t;
-    st(out, ts * G + tt * F);
+    if (toric) {
+      st(out, F);  // toric: H(x, t) = F(x; u·t^w)
+    } else {
+      c64 ts = gamma() * t, tt = C64(1.0) - t;
+      st(out, ts * G + tt * F);
+    }
     ++c_eval;
   }
   // H and its Jacobian (:106-124) in arithmetic T for the Jacobian
   template <class T>
   __device__ HC_NI void H_eval_jac(const c64* xv, c64 t) {
     HC_PHASE(PH_EVALJ);
+    if (toric) toric_coeffs(t.re);
     eval_mono64(xv);
     if constexpr (std::is_same<T, c32>::value) eval_mono32(xv);
     c64 F, G;
     val_rows64(F, G);
     c64 ts = gamma() * t, tt = C64(1.0) - t;
-    st(r, ts * G + tt * F);
+    if (toric)
+      st(r, F);
+    else
+      st(r, ts * G + tt * F);
     jac_rows<T>(ts, tt);
     Aprec = std::is_same<T, c32>::value ? 32 : 64;
     st(xJ, ld(xv));
@@ -540,6 +567,7 @@ struct PathTracker {
   // double-double residual (:81-94), rounded to FP64 on store
   __device__ HC_NI void H_eval_dd(const c64* xv, c64 t, c64* out) {
     HC_PHASE(PH_DD);
+    if (toric) toric_coeffs(t.re);
     __syncwarp();
     cdd* md = (cdd*)mono64;
     if (LANE == 0) md[0] = cdd_of(C64(1.0));
@@ -557,7 +585,7 @@ struct PathTracker {
     for (int s = s0; s < s1e; ++s) {
       int4 g = __ldg(R.seg + s);
       cdd acc = cdd_of(C64(0.0));
-      for (int tt = g.y; tt < g.z; ++tt) acc = acc + cdd_of(vcoef64[tt]) * md[vmono[tt]];
+      for (int tt = g.y; tt < g.z; ++tt) acc = acc + cdd_of(vc[tt]) * md[vmono[tt]];
       pp[g.w & 0xffffff] = acc;
     }
     __syncwarp();
@@ -565,11 +593,77 @@ struct PathTracker {
       cdd F = cdd_of(C64(0.0)), G = cdd_of(C64(0.0));
       for (int k = __ldg(R.row_slot + LANE); k < __ldg(R.row_slot + LANE + 1); ++k) F = F + pp[k];
       for (int k = __ldg(R.row_slot + n + LANE); k < __ldg(R.row_slot + n + LANE + 1); ++k) G = G + pp[k];
-      cdd ts = cdd_of(gamma() * t), tt = cdd_of(C64(1.0) - t);
-      out[LANE] = round_c(ts * G + tt * F);
+      if (toric) {
+        out[LANE] = round_c(F);
+      } else {
+        cdd ts = cdd_of(gamma() * t), tt = cdd_of(C64(1.0) - t);
+        out[LANE] = round_c(ts * G + tt * F);
+      }
     }
     __syncwarp();
     ++c_evaldd;
+  }
+
+  // coeffs! (src/homotopies/toric_homotopy.jl:147-180) for real t ≥ 0: c = u·t^w, t^w = exp(w log t)
+  __device__ HC_NI void toric_coeffs(double t) {
+    if (t == tc_t) return;
+    __syncwarp();
+    const int T = a->L.tor_n;
+    const double lt = log(t);
+    for (int k = LANE; k < T; k += 32) {
+      const double w = tw[k];
+      const double p = (t == 0.0) ? (w == 0.0 ? 1.0 : 0.0) : exp(w * lt);
+      tpow[k] = p;
+      tcoef[k] = vcoef64[k] * p;
+    }
+    tc_t = t;
+    __syncwarp();
+  }
+  // taylor! of the toric homotopy (src/homotopies/toric_homotopy.jl:181-278): the K-th Taylor
+  // coefficient of F(x(t+ε); c(t+ε)), u_i = Σ_k Σ_{j=0..K} c_k^(j) m_k^(K−j), with the
+  // coefficient series c^(j) = u·binom(w, j)·t^(w−j) (K = 1: c' = w·c/t; t = 0: the limits the
+  // reference takes) and the monomial series of orders 0..K (a toric program keeps all four
+  // orders of every monomial)
+  __device__ HC_NI void taylor_rows_toric(int K, double t, c64* out) {
+    toric_coeffs(t);
+    const c64* S = mono64;
+    const DevRows& R = P->val;
+    c64* pp = (c64*)part;
+    const bool at0 = (t == 0.0);
+    const double ti = 1.0 / t;
+    int s0 = __ldg(R.lane_seg + LANE), s1e = __ldg(R.lane_seg + LANE + 1);
+    for (int s = s0; s < s1e; ++s) {
+      int4 g = __ldg(R.seg + s);
+      c64 acc = C64(0.0);
+      for (int k = g.y; k < g.z; ++k) {
+        const c64* Sm = S + (int)vmono[k] * 4;
+        const double w = tw[k];
+        const c64 u0 = vcoef64[k];
+        if (K == 1) {
+          const c64 d = at0 ? (w == 1.0 ? u0 : C64(0.0)) : (w * tcoef[k]) * ti;
+          acc = cfma(d, Sm[0], acc);
+        } else {
+          double pw[4];
+          if (at0) {
+            pw[0] = w < 1e-12 ? 1.0 : 0.0;
+            pw[1] = (pw[0] == 0.0 && fabs(w - 1.0) <= 0x1p-26 * fmax(fabs(w), 1.0)) ? 1.0 : 0.0;
+            pw[2] = pw[3] = 0.0;
+          } else {
+            pw[0] = tpow[k];
+            pw[1] = w * pw[0] * ti;
+            pw[2] = 0.5 * (w - 1) * pw[1] * ti;
+            pw[3] = (w - 2) * pw[2] * ti / 3;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (j <= K) acc = cfma(u0 * pw[j], Sm[K - j], acc);
+        }
+      }
+      pp[g.w & 0xffffff] = acc;
+    }
+    __syncwarp();
+    if (LANE < n) out[LANE] = row_sum(R, pp, LANE);
+    __syncwarp();
   }
 
   // Taylor series of the homotopy in arithmetic T.
@@ -640,6 +734,13 @@ struct PathTracker {
         }
       }
       __syncwarp();
+    }
+    if constexpr (!F32) {
+      if (toric) {
+        taylor_rows_toric(K, t.re, out);
+        c_taylor += K;
+        return true;
+      }
     }
     const DevRows& R = P->val;
     T* pp = (T*)part;
@@ -1610,7 +1711,8 @@ struct PathTracker {
   }
 
   // init! (:639-754); returns is_tracking
-  __device__ HC_NI bool tracker_init(c64 t1, c64 t0) {
+  // ω and μ given (not NaN) skip init_newton, as init!'s keywords do
+  __device__ HC_NI bool tracker_init(c64 t1, c64 t0, double omega_in = dNaN(), double mu_in = dNaN()) {
     HC_PHASE(PH_INIT);
     phi_valid = false;
     step_logf = 0.f;
@@ -1632,13 +1734,15 @@ struct PathTracker {
     accepted_steps = rejected_steps = ext_accepted_steps = ext_rejected_steps = 0;
     last_steps_failed = 0;
     c64 t = ss.t();
-    bool valid;
-    double om, m_;
+    bool valid = true;
+    double om = omega_in, m_ = mu_in;
     bool ext = false;
-    init_newton(valid, om, m_, x, t, false);
-    if (!valid) {
-      ext = true;
-      init_newton(valid, om, m_, x, t, true);
+    if (isnan(om) || isnan(m_)) {
+      init_newton(valid, om, m_, x, t, false);
+      if (!valid) {
+        ext = true;
+        init_newton(valid, om, m_, x, t, true);
+      }
     }
     used_extended_prec = extended_prec = ext;
     if (!isnan(om)) omega = om;
@@ -2379,7 +2483,17 @@ struct PathTracker {
       }
     } else {
       c64 t1 = C64(a->t1_re, a->t1_im), t0 = C64(a->t0_re, a->t0_im);
-      tracker_init(t1, t0);
+      if (a->path_t1) t1 = C64(a->path_t1[k], 0.0);
+      if (a->path_t0) t0 = C64(a->path_t0[k], 0.0);
+      const double om_in = a->path_omega ? a->path_omega[k] : dNaN();
+      const double mu_in = a->path_mu ? a->path_mu[k] : dNaN();
+      if (toric) {
+        const double* wr = a->tor_w + (size_t)a->tor_row[k] * a->L.tor_n;
+        for (int j = LANE; j < a->L.tor_n; j += 32) tw[j] = wr[j];
+        tc_t = dNaN();
+        __syncwarp();
+      }
+      tracker_init(t1, t0, om_in, mu_in);
       while (tcode == TC_tracking) {
         tracker_step();
         if (cancelled()) {

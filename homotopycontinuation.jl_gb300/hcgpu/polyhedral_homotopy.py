@@ -1,0 +1,552 @@
+"""Polyhedral start systems and the polyhedral homotopy (src/polyhedral.jl) on the GPU tracker.
+
+Solving F by the polyhedral method (Huber and Sturmfels 1995) takes three parts:
+
+* mixed cells of a random integer lifting of F's supports — the reference takes them from
+  MixedSubdivisions.jl (a dependency outside the reference tree, pinned by its compat entry
+  "MixedSubdivisions 1"); :func:`fine_mixed_cells` restates the published method: a cell picks
+  one edge {a_i, b_i} of every lifted support such that some inner normal (γ, 1) is minimised
+  on exactly that edge in every support. A depth-first search over the supports with a linear
+  feasibility test per partial choice finds all of them; the mixed volume is the sum of the
+  cells' volumes |det(a_i − b_i)|.
+* the start solutions of every cell: a binomial system x^(a_i − b_i) = −c_{b_i}/c_{a_i}
+  (src/binomial_system.jl), solved here through a Hermite normal form in logarithmic
+  coordinates and refined there (:func:`solve_binomial`);
+* tracking: the toric homotopy H(x, t) = F(x; u ∘ t^w) from t = 0 to 1 for every start
+  solution (ToricHomotopy, tracked by hc_track_toric in FP64, one launch for all cells), then
+  the coefficient homotopy from the random start coefficients u to F's coefficients with the
+  endgame (CoefficientHomotopy = the straight-line homotopy with γ = 1, one launch).
+
+``only_non_zero = False`` (the default) adds the constant monomial to every support without
+one, so that solutions with zero coordinates are found too (Li and Wang 1996), exactly as
+src/polyhedral.jl:352-376 does.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from .systems import System, TotalDegreeHomotopy
+from .tracking import EndgameOptions, EndgameTracker, PathResult, Result, TrackerOptions, _Handle, make_options
+
+
+# --------------------------------------------------------------------------------------
+# supports
+# --------------------------------------------------------------------------------------
+def support_coefficients(F: System):
+    """Per equation the exponent matrix (terms × n) and the coefficients."""
+    return [np.asarray(e, dtype=np.int64) for e in F.exponents], [np.asarray(c, dtype=np.complex128)
+                                                                  for c in F.coefficients]
+
+
+def _has_zero_row(A):
+    return bool((np.asarray(A) == 0).all(axis=1).any())
+
+
+def _square_check(F: System):
+    from .parameters import FiniteException
+
+    if F.nequations < F.n:
+        raise FiniteException(F.n - F.nequations)
+    if F.nequations > F.n:
+        raise NotImplementedError("overdetermined systems (square_up) are not supported by the GPU solver")
+
+
+# --------------------------------------------------------------------------------------
+# mixed cells
+# --------------------------------------------------------------------------------------
+@dataclass
+class MixedCell:
+    """One cell of a fine mixed subdivision: ``indices[i] = (a_i, b_i)`` term indices of
+    support i, the inner normal γ (``normal``), β_i = min over support i of ⟨a, γ⟩ + ω(a), and
+    the normalized volume |det(a_i − b_i)|."""
+
+    indices: list
+    normal: np.ndarray
+    beta: np.ndarray
+    volume: int
+
+
+def _lp_margin(Aeq, beq, Aub, bub, n):
+    """max s subject to Aeq γ = beq, Aub γ + s ≤ bub, s ≤ 1 (γ free); −inf if infeasible."""
+    from scipy.optimize import linprog
+
+    nv = n + 1
+    c = np.zeros(nv)
+    c[-1] = -1.0
+    A_ub = np.hstack([Aub, np.ones((Aub.shape[0], 1))]) if len(Aub) else None
+    A_eq = np.hstack([Aeq, np.zeros((Aeq.shape[0], 1))]) if len(Aeq) else None
+    bounds = [(None, None)] * n + [(None, 1.0)]
+    r = linprog(c, A_ub=A_ub, b_ub=bub if len(Aub) else None, A_eq=A_eq, b_eq=beq if len(Aeq) else None,
+                bounds=bounds, method="highs")
+    if r.status != 0:
+        return -math.inf
+    return -r.fun
+
+
+def _edge_rows(S, w, p, q):
+    """Constraints of 'edge {p, q} of the lifted support (S, w) is where (γ, 1) is minimal'."""
+    eq_row = (S[p] - S[q]).astype(np.float64)
+    eq_rhs = float(w[q] - w[p])
+    others = [c for c in range(len(S)) if c != p and c != q]
+    ub = (S[p][None, :] - S[others]).astype(np.float64) if others else np.zeros((0, S.shape[1]))
+    ub_rhs = (w[others] - w[p]).astype(np.float64) if others else np.zeros(0)
+    return eq_row, eq_rhs, ub, ub_rhs
+
+
+class _DegenerateLifting(Exception):
+    pass
+
+
+def _mixed_cells_for_lifting(supports, lifting, tol):
+    n = supports[0].shape[1]
+    m = len(supports)
+    # lower edges of each lifted support
+    edges = []
+    for S, w in zip(supports, lifting):
+        E = []
+        for p in range(len(S)):
+            for q in range(p + 1, len(S)):
+                er, eb, U, ub = _edge_rows(S, w, p, q)
+                if not er.any():
+                    continue
+                if _lp_margin(er[None, :], np.array([eb]), U, ub, n) > tol:
+                    E.append((p, q, er, eb, U, ub))
+        edges.append(E)
+    order = sorted(range(m), key=lambda i: len(edges[i]))
+    cells = []
+    chosen = [None] * m
+
+    def rec(depth, Aeq, beq, Aub, bub):
+        if depth == m:
+            M = np.array(Aeq)
+            vol = int(round(abs(np.linalg.det(M))))
+            if vol == 0:
+                return
+            g = np.linalg.solve(M, np.array(beq))
+            # fine cell: every other lifted point lies strictly above the face
+            slack = np.array(bub) - np.array(Aub) @ g if len(Aub) else np.array([1.0])
+            eps = tol * max(1.0, np.abs(g).max())
+            if slack.min() < -eps:
+                return
+            if slack.min() <= eps:
+                raise _DegenerateLifting()
+            beta = np.array([float(supports[i][chosen[i][0]] @ g + lifting[i][chosen[i][0]]) for i in range(m)])
+            cells.append(MixedCell(indices=[tuple(chosen[i]) for i in range(m)], normal=g, beta=beta, volume=vol))
+            return
+        i = order[depth]
+        for (p, q, er, eb, U, ub) in edges[i]:
+            Aeq2 = Aeq + [er]
+            beq2 = beq + [eb]
+            Aub2 = Aub + list(U)
+            bub2 = bub + list(ub)
+            if depth + 1 < m:
+                if np.linalg.matrix_rank(np.array(Aeq2)) < len(Aeq2):
+                    continue
+                if _lp_margin(np.array(Aeq2), np.array(beq2), np.array(Aub2).reshape(-1, n), np.array(bub2), n) <= tol:
+                    continue
+            chosen[i] = (p, q)
+            rec(depth + 1, Aeq2, beq2, Aub2, bub2)
+            chosen[i] = None
+
+    rec(0, [], [], [], [])
+    return cells
+
+
+def fine_mixed_cells(supports, lifting=None, seed: Optional[int] = None, max_lift: int = 2 ** 12, tol: float = 1e-7,
+                     max_tries: int = 8):
+    """(cells, lifting) of a fine mixed subdivision of the supports (list of terms × n integer
+    arrays) under a random integer lifting (or the given one). A lifting that turns out
+    non-generic is drawn again."""
+    supports = [np.asarray(S, dtype=np.int64) for S in supports]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for _ in range(max_tries):
+        lift = [np.asarray(w, dtype=np.int64) for w in lifting] if lifting is not None else \
+            [rng.integers(0, max_lift, size=len(S)) for S in supports]
+        try:
+            return _mixed_cells_for_lifting(supports, lift, tol), lift
+        except _DegenerateLifting:
+            if lifting is not None:
+                raise ValueError("the given lifting does not induce a fine mixed subdivision")
+    raise RuntimeError("no generic lifting found")
+
+
+def _prepared_supports(supports, only_non_zero: bool):
+    if only_non_zero:
+        return [S - S.min(axis=0, keepdims=True) for S in supports]
+    return [S if _has_zero_row(S) else np.vstack([S, np.zeros((1, S.shape[1]), dtype=S.dtype)]) for S in supports]
+
+
+def mixed_volume(F_or_supports, only_non_zero: bool = True, seed: Optional[int] = 0) -> int:
+    """Mixed volume of the Newton polytopes (MixedSubdivisions.mixed_volume; with
+    only_non_zero = False of the supports with 0 added, the polyhedral path count)."""
+    sup = support_coefficients(F_or_supports)[0] if isinstance(F_or_supports, System) else \
+        [np.asarray(S, dtype=np.int64) for S in F_or_supports]
+    cells, _ = fine_mixed_cells(_prepared_supports(sup, only_non_zero), seed=seed)
+    return int(sum(c.volume for c in cells))
+
+
+# --------------------------------------------------------------------------------------
+# binomial systems (src/binomial_system.jl)
+# --------------------------------------------------------------------------------------
+def hnf(A):
+    """Lower-triangular column Hermite normal form: (H, U) with A U = H, U unimodular, H lower
+    triangular with positive diagonal and 0 ≤ H[i, j] < H[i, i] left of it (exact integers)."""
+    A = [[int(v) for v in row] for row in np.asarray(A)]
+    n = len(A)
+    H = [row[:] for row in A]
+    U = [[int(i == j) for j in range(n)] for i in range(n)]
+
+    def colop(j, k, a, b, c, d):  # (col j, col k) ← (a·col j + b·col k, c·col j + d·col k)
+        for M in (H, U):
+            for r in range(n):
+                x, y = M[r][j], M[r][k]
+                M[r][j], M[r][k] = a * x + b * y, c * x + d * y
+
+    for i in range(n):
+        for k in range(i + 1, n):
+            if H[i][k] == 0:
+                continue
+            x, y = H[i][i], H[i][k]
+            # extended gcd: g = s x + t y; new col i = s·ci + t·ck, new col k = (−y/g)·ci + (x/g)·ck
+            g, s, t = _egcd(x, y)
+            colop(i, k, s, t, -y // g, x // g)
+        if H[i][i] < 0:
+            for M in (H, U):
+                for r in range(n):
+                    M[r][i] = -M[r][i]
+        if H[i][i] == 0:
+            raise ValueError("singular matrix")
+        for j in range(i):
+            q = H[i][j] // H[i][i]
+            if q:
+                for M in (H, U):
+                    for r in range(n):
+                        M[r][j] -= q * M[r][i]
+    return np.array(H, dtype=object), np.array(U, dtype=object)
+
+
+def _egcd(a, b):
+    """(g, s, t) with g = s a + t b = gcd(a, b) > 0."""
+    old_r, r, old_s, s, old_t, t = a, b, 1, 0, 0, 1
+    while r:
+        q = old_r // r
+        old_r, r = r, old_r - q * r
+        old_s, s = s, old_s - q * s
+        old_t, t = t, old_t - q * t
+    if old_r < 0:
+        old_r, old_s, old_t = -old_r, -old_s, -old_t
+    return old_r, old_s, old_t
+
+
+def solve_binomial(A, b, refine: int = 3):
+    """All |det A| solutions x ∈ (C*)^n of x^{A[:, i]} = b_i (column i of A holds the exponents
+    of equation i), as the columns of an n × |det A| array (src/binomial_system.jl:1-476).
+
+    In logarithmic coordinates z = log x the system is linear, Aᵀ z = log b + 2πi k. With the
+    Hermite form Aᵀ U = H (lower triangular) and z = U y, row i reads
+    H_ii y_i = log b_i − Σ_{j<i} H_ij y_j + 2πi k_i, k_i = 0..H_ii−1. The solutions are refined
+    by Newton steps on the linear system (residual angles reduced to (−π, π])."""
+    A = np.asarray(A, dtype=np.int64)
+    b = np.asarray(b, dtype=np.complex128)
+    n = A.shape[0]
+    M = A.T
+    H, U = hnf(M)
+    Hf = np.array(H, dtype=np.float64)
+    Uf = np.array(U, dtype=np.float64)
+    Mf = M.astype(np.float64)
+    logb = np.log(b)
+    diag = [int(H[i][i]) for i in range(n)]
+    sols = []
+    for ks in np.ndindex(*diag):
+        y = np.zeros(n, dtype=np.complex128)
+        for i in range(n):
+            acc = logb[i] - np.dot(Hf[i, :i], y[:i]) + 2j * np.pi * ks[i]
+            y[i] = acc / Hf[i, i]
+        z = Uf @ y
+        for _ in range(refine):
+            # angles reduced first: the residual then involves numbers of size |A|·π only
+            z = z.real + 1j * (np.mod(z.imag + np.pi, 2 * np.pi) - np.pi)
+            r = Mf @ z - logb
+            r = r.real + 1j * (np.mod(r.imag + np.pi, 2 * np.pi) - np.pi)
+            z = z - np.linalg.solve(Mf, r)
+        sols.append(np.exp(z))
+    return np.array(sols).T.reshape(n, -1)
+
+
+# --------------------------------------------------------------------------------------
+# start solutions and weights of the toric homotopy
+# --------------------------------------------------------------------------------------
+def rand_approx_unit(rng, k):
+    """(0.9 + 0.2 u) · cis(2π v), u, v uniform (src/polyhedral.jl:336-343)."""
+    r = 0.9 + 0.2 * rng.random(k)
+    return r * np.exp(2j * np.pi * rng.random(k))
+
+
+def cell_start_solutions(supports, coeffs, cell: MixedCell) -> np.ndarray:
+    """Solutions (rows) of the cell's binomial system Σ_{a ∈ {a_i, b_i}} c_a x^a = 0."""
+    n = supports[0].shape[1]
+    A = np.zeros((n, n), dtype=np.int64)
+    bb = np.zeros(n, dtype=np.complex128)
+    for i, (p, q) in enumerate(cell.indices):
+        A[:, i] = supports[i][p] - supports[i][q]
+        bb[i] = -coeffs[i][q] / coeffs[i][p]
+    return solve_binomial(A, bb).T
+
+
+def cell_weights(supports, lifting, cell: MixedCell, min_weight=None, max_weight=None):
+    """update_weights! (src/homotopies/toric_homotopy.jl:62-104): per term of the flattened
+    supports w = ω − β_i + ⟨a, γ⟩ (0 on the cell's terms), scaled so that the smallest
+    non-cell weight is min_weight or the largest max_weight. Returns (w, s_min, s_max)."""
+    ws = []
+    s_max, s_min = 0.0, math.inf
+    for i, S in enumerate(supports):
+        a_i, b_i = cell.indices[i]
+        for j in range(len(S)):
+            if j == a_i or j == b_i:
+                ws.append(0.0)
+            else:
+                s = float(lifting[i][j]) - cell.beta[i]
+                for k in range(S.shape[1]):
+                    s += float(S[j, k]) * cell.normal[k]
+                ws.append(s)
+                s_max = max(s_max, s)
+                s_min = min(s_min, s)
+    w = np.array(ws)
+    if min_weight is not None:
+        lam = s_min / min_weight
+        w = w / lam
+        s_min, s_max = min_weight, s_max / lam
+    elif max_weight is not None:
+        lam = s_max / max_weight
+        w = w / lam
+        s_min, s_max = s_min / lam, max_weight
+    return w, s_min, s_max
+
+
+@dataclass
+class PolyhedralStartSolutions:
+    """The start solutions of the polyhedral homotopy: (cell index, x) pairs
+    (PolyhedralStartSolutionsIterator, src/polyhedral.jl:7-49)."""
+
+    supports: list
+    start_coefficients: list
+    lifting: list
+    cells: list
+    cell_of: np.ndarray = field(default=None)
+    x: np.ndarray = field(default=None)
+
+    def __post_init__(self):
+        if self.x is None:
+            xs, cs = [], []
+            for k, c in enumerate(self.cells):
+                X = cell_start_solutions(self.supports, self.start_coefficients, c)
+                xs.append(X)
+                cs.extend([k] * len(X))
+            n = self.supports[0].shape[1]
+            self.x = np.concatenate(xs, axis=0) if xs else np.zeros((0, n), dtype=np.complex128)
+            self.cell_of = np.asarray(cs, dtype=np.int32)
+
+    def __len__(self):
+        return len(self.x)
+
+    def __iter__(self):
+        for k in range(len(self.x)):
+            yield (self.cells[self.cell_of[k]], self.x[k])
+
+
+def _flat_system(supports, coeffs, n) -> System:
+    return System([np.asarray(S, dtype=np.int32) for S in supports], [np.asarray(c) for c in coeffs], nvars=n)
+
+
+class PolyhedralTracker:
+    """Two-stage tracker of the polyhedral homotopy (PolyhedralTracker, src/polyhedral.jl:412-530):
+    the toric homotopy from t = 0 (binomial system) to 1 (the generic system with the start
+    coefficients), restarted with weights rescaled to a maximum of 10 when the cell's largest
+    weight is ≥ 10, then the coefficient homotopy to F with the endgame. Every stage is one
+    launch over all paths."""
+
+    def __init__(self, supports, start_coeffs, target_coeffs, lifting, cells, n,
+                 tracker_options: Optional[TrackerOptions] = None, endgame_options: Optional[EndgameOptions] = None):
+        self.supports = supports
+        self.start_coeffs = start_coeffs
+        self.target_coeffs = target_coeffs
+        self.lifting = lifting
+        self.cells = cells
+        self.n = n
+        self.tracker_options = tracker_options or TrackerOptions()
+        self.endgame_options = endgame_options or EndgameOptions()
+        self.generic_start = _flat_system(supports, start_coeffs, n)
+        self.target = _flat_system(supports, target_coeffs, n)
+        # stage-1 weights (min weight 1) and restart weights (max weight 10) per cell
+        W1, W2, wmax = [], [], []
+        for c in cells:
+            w1, _, s_max1 = cell_weights(supports, lifting, c, min_weight=1.0)
+            w2, s_min2, _ = cell_weights(supports, lifting, c, max_weight=10.0)
+            W1.append(w1)
+            W2.append(w2)
+            wmax.append((s_max1, s_min2))
+        self.W1 = np.array(W1).reshape(len(cells), -1)
+        self.W2 = np.array(W2).reshape(len(cells), -1)
+        self.wmax = wmax
+        self._last_toric = None
+
+    def _toric_handle(self, W, options):
+        h = _Handle(options)
+        eq, ex, cf = self.generic_start.term_arrays()
+        P = _lib.ptr
+        h._keep = (eq, ex, cf, W)
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        _lib.check(h.L.hc_set_toric(h.h, self.n, len(eq), P(eq), P(ex), P(cf), W.shape[0], P(W)), h.h)
+        h.n = self.n
+        return h
+
+    def _toric_track(self, h, x, rows, t1, t0, omega=None, mu=None):
+        x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1, self.n)
+        k = len(x)
+        res = np.zeros(k, dtype=_lib.RESULT_DTYPE)
+        sol = np.zeros((k, self.n), dtype=np.complex128)
+        P = _lib.ptr
+        args = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (t1, t0, omega, mu)]
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        if k:
+            _lib.check(h.L.hc_track_toric(h.h, k, P(x), P(rows), P(args[0]), P(args[1]), P(args[2]), P(args[3]),
+                                          P(res), P(sol)), h.h)
+        return res, sol
+
+    def track_toric(self, starts: PolyhedralStartSolutions):
+        """Stage 1 (and its restart): per path (return code, x at t = 1, ω, μ, steps)."""
+        to = self.tracker_options
+        x = starts.x
+        rows = starts.cell_of
+        npaths = len(x)
+        smax = np.array([self.wmax[c][0] for c in rows]) if npaths else np.zeros(0)
+        split = smax >= 10
+        t_end = np.where(split, np.clip(0.1 ** (10.0 / np.where(split, smax, 1.0)), 0.9, 1 - 1e-6), 1.0)
+        o1 = make_options(to, None)
+        o1.max_initial_step_size = 0.2
+        h1 = self._toric_handle(self.W1, o1)
+        res, sol = self._toric_track(h1, x, rows, np.zeros(npaths), t_end, np.full(npaths, 20.0),
+                                     np.full(npaths, 1e-12))
+        codes = res["return_code"].copy()
+        acc = res["accepted_steps"].copy()
+        rej = res["rejected_steps"].copy()
+        omega = res["omega"].copy()
+        mu = res["mu"].copy()
+        # restart with weights rescaled to a maximum of 10 (src/polyhedral.jl:455-484)
+        idx = np.nonzero(split & (codes == _TRACKER_SUCCESS))[0]
+        if len(idx):
+            o2 = make_options(to, None)
+            o2.min_step_size = 0.0
+            h2 = self._toric_handle(self.W2, o2)
+            smin2 = np.array([self.wmax[c][1] for c in rows[idx]])
+            t_restart = t_end[idx] ** (1.0 / smin2)
+            r2, s2 = self._toric_track(h2, sol[idx], rows[idx], t_restart, np.ones(len(idx)), omega[idx], mu[idx])
+            codes[idx] = r2["return_code"]
+            sol[idx] = s2
+            acc[idx] += r2["accepted_steps"]
+            rej[idx] += r2["rejected_steps"]
+            omega[idx] = r2["omega"]
+            mu[idx] = r2["mu"]
+        self._last_toric = dict(codes=codes, accepted=acc, rejected=rej, omega=omega, mu=mu)
+        return codes, sol, acc, rej, mu
+
+    def track_arrays(self, starts: PolyhedralStartSolutions):
+        """Both stages; returns (PathResult list in start order)."""
+        codes, x1, acc, rej, mu = self.track_toric(starts)
+        ok = codes == _TRACKER_SUCCESS
+        H = TotalDegreeHomotopy(F=self.target, G=self.generic_start, gamma=1.0 + 0j, degrees=self.target.degrees(),
+                                scaling=np.ones(self.n))
+        E = EndgameTracker(H, self.tracker_options, self.endgame_options)
+        out: List[Optional[PathResult]] = [None] * len(x1)
+        idx = np.nonzero(ok)[0]
+        if len(idx):
+            prs = E.track_batch(x1[idx], path_numbers=idx + 1)
+            for j, k in enumerate(idx):
+                r = prs[j]
+                r.start_solution = starts.x[k]
+                r.accepted_steps += int(acc[k])
+                r.rejected_steps += int(rej[k])
+                out[k] = r
+        for k in np.nonzero(~ok)[0]:
+            out[k] = PathResult(return_code="polyhedral_failed", solution=x1[k].copy(), t=float("nan"),
+                                accuracy=float("nan"), residual=float("nan"), singular=False,
+                                condition_jacobian=float("nan"), winding_number=None, extended_precision=False,
+                                path_number=int(k + 1), start_solution=starts.x[k], last_path_point=None,
+                                valuation=None, omega=float(self._last_toric["omega"][k]), mu=float(mu[k]),
+                                accepted_steps=int(acc[k]), rejected_steps=int(rej[k]), steps_eg=0,
+                                extended_precision_used=False)
+        return out
+
+    def track(self, start, path_number=None) -> PathResult:
+        """track(PT, (cell, x)) for one start solution."""
+        cell, x = start
+        k = next(i for i, c in enumerate(self.cells) if c is cell)
+        one = PolyhedralStartSolutions(self.supports, self.start_coeffs, self.lifting, self.cells,
+                                       cell_of=np.array([k], dtype=np.int32), x=np.asarray(x)[None, :])
+        r = self.track_arrays(one)[0]
+        r.path_number = path_number
+        return r
+
+
+_TRACKER_SUCCESS = 1  # TrackerCode.success
+
+
+def polyhedral(F: System, *, only_non_zero: bool = False, only_torus: Optional[bool] = None,
+               seed: Optional[int] = None, tracker_options: Optional[TrackerOptions] = None,
+               endgame_options: Optional[EndgameOptions] = None, start_coefficients=None):
+    """polyhedral(F; only_non_zero, tracker_options, endgame_options) (src/polyhedral.jl:197-408):
+    (PolyhedralTracker, PolyhedralStartSolutions)."""
+    if only_torus is not None:
+        only_non_zero = only_torus
+    _square_check(F)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    supports, target = support_coefficients(F)
+    n = F.n
+    if start_coefficients is None:
+        start = [rand_approx_unit(rng, len(c)) * np.max(np.abs(c)) for c in target]
+    else:
+        start = [np.asarray(c, dtype=np.complex128) for c in start_coefficients]
+    if only_non_zero:
+        supports = [S - S.min(axis=0, keepdims=True) for S in supports]
+    else:
+        sup2, st2, tg2 = [], [], []
+        for S, cs, ct_ in zip(supports, start, target):
+            if _has_zero_row(S):
+                sup2.append(S)
+                st2.append(cs)
+                tg2.append(ct_)
+            else:
+                sup2.append(np.vstack([S, np.zeros((1, n), dtype=S.dtype)]))
+                z = (rng.standard_normal() + 1j * rng.standard_normal()) / np.sqrt(2)
+                st2.append(np.append(cs, z))
+                tg2.append(np.append(ct_, 0.0))
+        supports, start, target = sup2, st2, tg2
+    cells, lifting = fine_mixed_cells(supports, seed=None if seed is None else seed + 7)
+    if not cells:
+        raise RuntimeError("Cannot compute a start system.")
+    starts = PolyhedralStartSolutions(supports, start, lifting, cells)
+    tracker = PolyhedralTracker(supports, start, target, lifting, cells, n, tracker_options, endgame_options)
+    return tracker, starts
+
+
+def paths_to_track(F: System, only_non_zero: bool = False, only_torus: Optional[bool] = None, seed=0) -> int:
+    """paths_to_track(F; start_system = :polyhedral) (src/polyhedral.jl:285-322)."""
+    if only_torus is not None:
+        only_non_zero = only_torus
+    _square_check(F)
+    return mixed_volume(F, only_non_zero=only_non_zero, seed=seed)
+
+
+def solve_polyhedral(F: System, *, only_non_zero: bool = False, seed: Optional[int] = None,
+                     tracker_options: Optional[TrackerOptions] = None,
+                     endgame_options: Optional[EndgameOptions] = None) -> Result:
+    """solve(F; start_system = :polyhedral): every start solution through both stages."""
+    T, S = polyhedral(F, only_non_zero=only_non_zero, seed=seed, tracker_options=tracker_options,
+                      endgame_options=endgame_options)
+    prs = T.track_arrays(S)
+    return Result(prs, seed=seed, start_system="polyhedral")

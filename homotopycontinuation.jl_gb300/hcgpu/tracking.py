@@ -473,8 +473,9 @@ def nfailed(R: Result):
 def solve(F, starts=None, start_system: str = "total_degree", *, start_parameters=None, target_parameters=None,
           transform_result=None, transform_parameters=None, flatten: bool = False, gamma=None, seed=None,
           tracker_options=None, endgame_options=None, precision: str = "fp64", step_control: str = "plain"):
-    """solve(F; start_system = :total_degree) (src/solve.jl:447-526): one batched GPU call
-    replaces threaded_solve's per-path loop (src/solve.jl:628-709).
+    """solve(F; start_system = :total_degree | :polyhedral) (src/solve.jl:447-526): one batched
+    GPU call replaces threaded_solve's per-path loop (src/solve.jl:628-709); the polyhedral start
+    system tracks its toric stage and its coefficient homotopy as one launch each.
 
     With ``start_parameters`` (F a parameters.ParametricSystem, ``starts`` its solutions at the
     start parameters): the parameter homotopy to ``target_parameters``; a list of target
@@ -488,8 +489,17 @@ def solve(F, starts=None, start_system: str = "total_degree", *, start_parameter
                                 endgame_options=endgame_options, transform_result=transform_result,
                                 transform_parameters=transform_parameters, flatten=flatten,
                                 precision=precision, step_control=step_control)
+    if start_system == "polyhedral":
+        from .polyhedral_homotopy import solve_polyhedral
+
+        if starts is not None:
+            raise NotImplementedError("start solutions without start_parameters (a start system G) are not supported")
+        to = tracker_options or TrackerOptions()
+        to.precision = precision
+        to.step_control = step_control
+        return solve_polyhedral(F, seed=seed, tracker_options=to, endgame_options=endgame_options)
     if start_system != "total_degree":
-        raise NotImplementedError("only start_system='total_degree' is supported")
+        raise NotImplementedError("start_system must be 'total_degree' or 'polyhedral'")
     if starts is not None:
         raise NotImplementedError("start solutions without start_parameters (a start system G) are not supported")
     to = tracker_options or TrackerOptions()

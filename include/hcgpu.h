@@ -125,6 +125,27 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
                     hc_path_result* d_results, double* d_solutions, double* d_valuation,
                     double* d_last, void* stream);
 
+/* Toric homotopy of the polyhedral method (ToricHomotopy, src/homotopies/toric_homotopy.jl:9-278;
+ * its tracking in PolyhedralTracker, src/polyhedral.jl:412-530):
+ *   H(x, t) = F(x; c(t)),  c_k(t) = u_k t^{w_k}
+ * with the base coefficients u of the term table (F_eq, F_exps, F_coef as in hc_set_homotopy;
+ * no start system) and per-path weights w: `weights` holds `nrows` rows of nF finite,
+ * non-negative weights in the table's term order (one row per mixed cell; 0 on the cell's
+ * own terms). The handle then tracks this homotopy only (hc_set_homotopy switches back). */
+int hc_set_toric(hc_handle* h, int n, int nF, const int32_t* F_eq, const int32_t* F_exps, const double* F_coef,
+                 int nrows, const double* weights);
+
+/* Track npaths start vectors of the toric homotopy with the plain Tracker in FP64 (track!,
+ * src/tracker.jl:937-965): path p uses weight row rows[p] and runs from t1[p] to t0[p]
+ * (real, ≥ 0); omega/mu (may be NULL; NaN entries allowed) are init!'s ω and μ keywords — both
+ * given skip init_newton. max_initial_step_size and min_step_size come from the options
+ * (stage 1 of the reference sets 0.2; its restart sets min_step_size 0).
+ * out_results[npaths] holds TrackerResult fields (return_code: TrackerCode), out_solutions
+ * the endpoints. Host buffers; returns when the results are on the host. */
+int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int32_t* rows, const double* t1,
+                   const double* t0, const double* omega, const double* mu, hc_path_result* out_results,
+                   double* out_solutions);
+
 /* Request cancellation of a running hc_track on this handle (thread-safe). Paths not yet
  * finished report TrackerCode terminated_unknown and hc_track returns HC_ERR_CANCELLED. */
 int hc_cancel(hc_handle* h);

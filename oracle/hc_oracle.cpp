@@ -300,15 +300,40 @@ static void sys_taylor(const System& F, int K, const C* tx, int nx, C* dv /* (K+
   }
 }
 
-// src/homotopies/straight_line_homotopy.jl: H(x,t) = γ t G(x) + (1-t) F(x)
+// src/homotopies/straight_line_homotopy.jl: H(x,t) = γ t G(x) + (1-t) F(x);
+// toric (src/homotopies/toric_homotopy.jl): H(x,t) = F(x; u·t^w), u = F's coefficients, w per term
 struct Homotopy {
   System G, F;
   C gamma;
   int n, m;
+  bool toric = false;
+  std::vector<double> w;     // weights of the current path (F's term order)
+  mutable System Ft;         // F with the coefficients u·t^w at t = tc_t
+  mutable std::vector<double> tpow;
+  mutable double tc_t = NaN;
 };
+
+// coeffs! (toric_homotopy.jl:147-180) for real t ≥ 0
+static const System& toric_sys(const Homotopy& H, double t) {
+  if (!(t == H.tc_t)) {
+    H.tpow.resize(H.F.terms.size());
+    for (size_t k = 0; k < H.F.terms.size(); ++k) {
+      double w = H.w[k];
+      double p = (t == 0.0) ? (w == 0.0 ? 1.0 : 0.0) : std::exp(w * std::log(t));
+      H.tpow[k] = p;
+      H.Ft.terms[k].coef = H.F.terms[k].coef * p;
+    }
+    H.tc_t = t;
+  }
+  return H.Ft;
+}
 
 // :96-104
 static void H_eval(const Homotopy& H, const C* x, C t, C* u) {
+  if (H.toric) {
+    sys_eval(toric_sys(H, t.re), x, u);
+    return;
+  }
   std::vector<C> g(H.m), f(H.m);
   sys_eval(H.G, x, g.data());
   sys_eval(H.F, x, f.data());
@@ -317,6 +342,12 @@ static void H_eval(const Homotopy& H, const C* x, C t, C* u) {
 }
 // :81-94 (DD residual rounded to F64 on store)
 static void H_eval_dd(const Homotopy& H, const CDD* x, C t, C* u) {
+  if (H.toric) {
+    std::vector<CDD> f(H.m);
+    sys_eval(toric_sys(H, t.re), x, f.data());
+    for (int i = 0; i < H.m; ++i) u[i] = round_c(f[i]);
+    return;
+  }
   std::vector<CDD> g(H.m), f(H.m);
   sys_eval(H.G, x, g.data());
   sys_eval(H.F, x, f.data());
@@ -325,6 +356,10 @@ static void H_eval_dd(const Homotopy& H, const CDD* x, C t, C* u) {
 }
 // :106-124
 static void H_eval_jac(const Homotopy& H, const C* x, C t, C* u, C* U) {
+  if (H.toric) {
+    sys_eval_jac(toric_sys(H, t.re), x, u, U);
+    return;
+  }
   int m = H.m, n = H.n;
   std::vector<C> g(m), f(m), Gj((size_t)m * n), Fj((size_t)m * n);
   sys_eval_jac(H.G, x, g.data(), Gj.data());
@@ -333,8 +368,22 @@ static void H_eval_jac(const Homotopy& H, const C* x, C t, C* u, C* U) {
   for (int i = 0; i < m; ++i) u[i] = ts * g[i] + tt * f[i];
   for (size_t k = 0; k < (size_t)m * n; ++k) U[k] = ts * Gj[k] + tt * Fj[k];
 }
-// :130-137  taylor!(u, Val(1), H, x, t) = γ G(x) - F(x)
-static void H_taylor1(const Homotopy& H, const C* x, C* u) {
+// :130-137  taylor!(u, Val(1), H, x, t) = γ G(x) - F(x);
+// toric (toric_homotopy.jl:133-146, 255-257): F(x; ċ), ċ = w·c/t (t = 0: u where w == 1)
+static void H_taylor1(const Homotopy& H, const C* x, C t, C* u) {
+  if (H.toric) {
+    const System& Fc = toric_sys(H, t.re);
+    System Fd = Fc;
+    for (size_t k = 0; k < Fd.terms.size(); ++k) {
+      double w = H.w[k];
+      if (t.re == 0.0)
+        Fd.terms[k].coef = (w == 1.0) ? H.F.terms[k].coef : cx(0.0);
+      else
+        Fd.terms[k].coef = (w * Fc.terms[k].coef) * (1.0 / t.re);
+    }
+    sys_eval(Fd, x, u);
+    return;
+  }
   std::vector<C> g(H.m), f(H.m);
   sys_eval(H.G, x, g.data());
   sys_eval(H.F, x, f.data());
@@ -343,6 +392,35 @@ static void H_taylor1(const Homotopy& H, const C* x, C* u) {
 // :138-154  taylor!(u, Val(K), H, tx, t), tx holds K vectors (orders 0..K-1)
 static void H_taylorK(const Homotopy& H, int K, const C* tx, C t, C* u) {
   int m = H.m;
+  if (H.toric) {
+    // taylor_coeffs! (toric_homotopy.jl:199-253): c^(j) = u·tw_j, tw_0 = t^w,
+    // tw_1 = w tw_0/t, tw_2 = (w-1)/2 tw_1/t, tw_3 = (w-2) tw_2/t/3; u_K = Σ_j [ε^(K-j)] F(x(ε); c^(j))
+    const double tr = t.re;
+    toric_sys(H, tr);
+    for (int i = 0; i < m; ++i) u[i] = cx(0.0);
+    std::vector<C> dv((size_t)(K + 1) * m);
+    for (int j = 0; j <= K; ++j) {
+      System Fj = H.F;
+      for (size_t k = 0; k < Fj.terms.size(); ++k) {
+        double w = H.w[k], tw[4];
+        if (tr == 0.0) {
+          tw[0] = w < 1e-12 ? 1.0 : 0.0;
+          tw[1] = (tw[0] == 0.0 && std::fabs(w - 1.0) <= 0x1p-26 * std::max(std::fabs(w), 1.0)) ? 1.0 : 0.0;
+          tw[2] = tw[3] = 0.0;
+        } else {
+          double ti = 1.0 / tr;
+          tw[0] = H.tpow[k];
+          tw[1] = w * tw[0] * ti;
+          tw[2] = 0.5 * (w - 1) * tw[1] * ti;
+          tw[3] = (w - 2) * tw[2] * ti / 3;
+        }
+        Fj.terms[k].coef = H.F.terms[k].coef * tw[j];
+      }
+      sys_taylor(Fj, K, tx, K, dv.data());
+      for (int i = 0; i < m; ++i) u[i] = u[i] + dv[(size_t)(K - j) * m + i];
+    }
+    return;
+  }
   std::vector<C> dg((size_t)(K + 1) * m), df((size_t)(K + 1) * m);
   sys_taylor(H.G, K, tx, K, dg.data());
   sys_taylor(H.F, K, tx, K, df.data());
@@ -959,7 +1037,7 @@ static void predictor_update(Predictor& P, const Homotopy& H, const C* x, C t, M
 
   const double* w = norm.w.data();
   // ẋ = -H_x⁻¹ H_t
-  H_taylor1(H, x, P.u.data());
+  H_taylor1(H, x, t, P.u.data());
   for (int i = 0; i < H.m; ++i) P.u[i] = -P.u[i];
   jac_ldiv(J, P.xtemp.data(), P.u.data(), nullptr);
   double delta = fp_refine_step(J, P.xtemp.data(), P.u.data(), w);
@@ -2205,6 +2283,69 @@ int hco_track(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const d
   return 0;
 }
 
+// Toric homotopy tracking of the polyhedral method (PolyhedralTracker's toric stage,
+// src/polyhedral.jl:439-484): path k tracks starts[k] from t1[k] to t0[k] with the weights of
+// row rows[k] (weights: nrows × nF, F's term order) and init!'s ω/μ keywords (NaN: init_newton).
+int hco_track_toric(int n, int nF, const int32_t* F_eq, const int32_t* F_exps, const double* F_coef, int nrows,
+                    const double* weights, int64_t npaths, const double* starts, const int32_t* rows,
+                    const double* t1, const double* t0, const double* omega, const double* mu,
+                    const hco_options* opts, int nthreads, hco_path_result* out, double* out_x) {
+  Homotopy H0;
+  H0.n = H0.m = n;
+  H0.F = make_system(n, n, nF, F_eq, F_exps, F_coef);
+  H0.G = make_system(n, n, 0, nullptr, nullptr, nullptr);
+  H0.gamma = cx(1.0);
+  H0.toric = true;
+  H0.Ft = H0.F;
+  (void)nrows;
+  TrackerOptions to;
+  EndgameOptions eo;
+  to_opts(opts, to, eo);
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  if (npaths < nthreads) nthreads = (int)std::max<int64_t>(1, npaths);
+  std::atomic<int64_t> next(0);
+  auto worker = [&]() {
+    Homotopy H = H0;
+    Tracker T;
+    T.setup(H, to);
+    std::vector<C> x0(n), r(n);
+    while (true) {
+      int64_t k = next.fetch_add(1);
+      if (k >= npaths) break;
+      for (int i = 0; i < n; ++i) x0[i] = C{starts[(k * n + i) * 2], starts[(k * n + i) * 2 + 1]};
+      H.w.assign(weights + (size_t)rows[k] * nF, weights + (size_t)(rows[k] + 1) * nF);
+      H.tc_t = NaN;
+      tracker_init(T, x0.data(), cx(t1[k]), cx(t0[k]), omega ? omega[k] : NaN, mu ? mu[k] : NaN);
+      while (T.code == TC_tracking) tracker_step(T);
+      C t = T.ss.t();
+      hco_path_result& R = out[k];
+      std::memset(&R, 0, sizeof(R));
+      R.path_number = k + 1;
+      R.return_code = T.code;
+      R.t_re = t.re;
+      R.t_im = t.im;
+      R.accuracy = T.accuracy;
+      R.omega = T.omega;
+      R.mu = T.mu;
+      R.tau = T.tau;
+      R.extended_precision = T.extended_prec || T.refined_extended_prec;
+      R.extended_precision_used = T.used_extended_prec || T.refined_extended_prec;
+      R.accepted_steps = T.accepted_steps;
+      R.rejected_steps = T.rejected_steps;
+      H_eval(H, T.x.data(), t, r.data());
+      R.residual = inf_norm_v(r.data(), n);
+      for (int i = 0; i < n; ++i) {
+        out_x[(k * n + i) * 2] = T.x[i].re;
+        out_x[(k * n + i) * 2 + 1] = T.x[i].im;
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int i = 0; i < nthreads; ++i) th.emplace_back(worker);
+  for (auto& t : th) t.join();
+  return 0;
+}
+
 // --- unit-level entry points for the known-answer tests ---------------------------------
 
 // LU + ldiv (src/linear_algebra.jl:389-408), A column-major n×n complex, b n complex
@@ -2280,7 +2421,7 @@ int hco_homotopy_eval(int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
     }
     return 0;
   } else if (kind == 3) {
-    H_taylor1(H, xv.data(), u.data());
+    H_taylor1(H, xv.data(), t, u.data());
   } else {
     H_taylorK(H, kind - 2, xv.data(), t, u.data());
   }

@@ -121,6 +121,11 @@ def lib():
             ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_double,
             ct.POINTER(Options), ct.c_int, P, P, P, P,
         ]
+        L.hco_track_toric.restype = ct.c_int
+        L.hco_track_toric.argtypes = [
+            ct.c_int, ct.c_int, P, P, P, ct.c_int, P, ct.c_int64, P, P, P, P, P, P,
+            ct.POINTER(Options), ct.c_int, P, P,
+        ]
         L.hco_ldiv.argtypes = [ct.c_int, P, P, P]
         L.hco_inverse_inf_norm_est.argtypes = [ct.c_int, P, P, P, P, P]
         L.hco_dd_op.argtypes = [ct.c_int, P, P, P]
@@ -176,6 +181,26 @@ def track(G_terms, F_terms, gamma, starts, *, endgame=True, t1=1.0, t0=0.0, opti
         _ptr(res), _ptr(xs), _ptr(val), _ptr(last),
     )
     return res, xs, val, last
+
+
+def track_toric(F_terms, weights, starts, rows, t1, t0, omega=None, mu=None, options=None, nthreads=0):
+    """Toric stage of the polyhedral method with the oracle: path k from t1[k] to t0[k] with
+    weight row rows[k] (weights: rows × terms of F_terms, in their order). Returns (results,
+    endpoints)."""
+    starts = _cplx(starts)
+    npaths, n = starts.shape
+    Fe, Fx, Fc = F_terms
+    W = np.ascontiguousarray(weights, dtype=np.float64)
+    opts = options if options is not None else default_options()
+    res = np.zeros(npaths, dtype=RESULT_DTYPE)
+    xs = np.zeros((npaths, n), dtype=np.complex128)
+    f64 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    t1, t0, omega, mu = f64(t1), f64(t0), f64(omega), f64(mu)
+    lib().hco_track_toric(n, len(Fe), _ptr(Fe), _ptr(Fx), _ptr(Fc), W.shape[0], _ptr(W), npaths, _ptr(starts),
+                          _ptr(rows), _ptr(t1), _ptr(t0), _ptr(omega), _ptr(mu), ct.byref(opts), int(nthreads),
+                          _ptr(res), _ptr(xs))
+    return res, xs
 
 
 def ldiv(A, b):
