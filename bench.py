@@ -2,7 +2,7 @@
 homotopy (59,049 paths), with the plain FP64 GPU tracker and the CPU oracle beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dense|sparse|uneven]
+                    [--workload dense|sparse|uneven|polyhedral]
 
 A "step" is one batched tracking call over all paths of the workload. Prints one JSON line.
 Under torchrun (N > 1) every rank tracks its own seeded instance (weak scaling) and rank 0
@@ -35,6 +35,8 @@ WORKLOADS = {
               "<= 4 plus a constant each), 65,536 paths, most diverging (endgame-heavy)",
     "uneven": "2,000 independent dense instances in one launch, n uniform in 3..8, each equation degree uniform "
               "in {2,3}, all total-degree paths of every instance",
+    "polyhedral": "polyhedral homotopy of the 8x8 sparse system of the sparse workload: mixed-volume many paths "
+                  "(toric stage, then the coefficient homotopy with the endgame)",
 }
 
 
@@ -168,7 +170,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload == "uneven":
+    if args.workload in ("uneven", "polyhedral"):
         print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable": "the reference CPU arm is timed on "
                           "the dense headline workload only"}), flush=True)
         return
@@ -225,6 +227,8 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.workload == "uneven":
         return main_uneven(args, torch, hc, _lib, local)
+    if args.workload == "polyhedral":
+        return main_polyhedral(args, torch, hc, _lib, local)
     H, S = workload(args.seed + rank, args.workload)
     if args.paths:
         S = S[: args.paths]
@@ -502,6 +506,86 @@ def main_uneven(args, torch, hc, _lib, local):
             "max_rel_endpoint_err_device_call_unchecked": err_device,
             "steps_per_path": float((res["accepted_steps"] + res["rejected_steps"]).mean()),
             "steps_per_path_plain_fp64": float((res64["accepted_steps"] + res64["rejected_steps"]).mean()),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main_polyhedral(args, torch, hc, _lib, local):
+    """solve(F; start_system = :polyhedral) of the 8x8 sparse system: mixed cells and start
+    solutions on the host (timed apart), then per step both tracking stages through the host
+    API (hc_track_toric, hc_track), with the total-degree solve of the same system beside it."""
+    from hcgpu import polyhedral_homotopy as ph
+
+    rank = int(os.environ.get("RANK", "0"))
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        raise SystemExit("--workload polyhedral runs on one GPU")
+    F, g = hc.sparse_random_system(8, 8, 4, seed=args.seed)
+    t = time.perf_counter()
+    T, S = ph.polyhedral(F, seed=args.seed + 1)
+    prep_s = time.perf_counter() - t
+    npaths = len(S)
+    for _ in range(args.warmup):
+        T.track_arrays(S)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        times = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            rs = T.track_arrays(S)
+            times.append(time.perf_counter() - t)
+    ms = 1000 * float(np.mean(times))
+    codes = [r.return_code for r in rs]
+    nonsing = sum(r.is_success() and not r.is_singular() for r in rs)
+    sing = sum(r.is_success() and r.is_singular() for r in rs)
+    # total degree on the same system (plain FP64, same options)
+    H = hc.total_degree_homotopy(F, g)
+    S2 = hc.total_degree_start_solutions(H.degrees)
+    E = hc.EndgameTracker(H, hc.TrackerOptions())
+    E.track_arrays(S2[:4096])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r2 = E.track_batch(S2)
+    td_s = time.perf_counter() - t
+    nonsing2 = sum(r.is_success() and not r.is_singular() for r in r2)
+    # CPU baseline: the oracle's polyhedral tracker on an evenly spaced sample of the paths
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import polyhedral_oracle as po
+
+        sample = min(args.cpu_sample, npaths)
+        idx = np.linspace(0, npaths - 1, sample).astype(np.int64)
+        sub = ph.PolyhedralStartSolutions(S.supports, S.start_coefficients, S.lifting, S.cells,
+                                          cell_of=S.cell_of[idx], x=S.x[idx])
+        cores = os.cpu_count()
+        t = time.perf_counter()
+        ocodes, ox, _ = po.track(T, sub, nthreads=cores)
+        dt = time.perf_counter() - t
+        agree = int(sum((ocodes[j] == 1) == rs[k].is_success() for j, k in enumerate(idx)))
+        cpu = {"value": sample / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} of {npaths} paths (evenly spaced), C++ FP64 restatement of the reference "
+                         f"PolyhedralTracker on {cores} threads, {dt:.1f} s; success flags agree on {agree}"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": npaths / (ms / 1000), "unit": "paths/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded complex Gaussian coefficients, N(0,1/2) re/im)",
+            "config": {"workload": WORKLOADS["polyhedral"], "seed": args.seed, "paths": npaths,
+                       "mixed_cells": len(T.cells), "host_preparation_seconds": prep_s,
+                       "timing": "host API per step (starts copied in, results copied out): value and e2e coincide",
+                       "precision": "fp64", "step_control": "plain"},
+            "e2e": {"value": npaths / (ms / 1000), "unit": "paths/s",
+                    "h2d_bytes_per_step": int(S.x.nbytes * 2), "d2h_bytes_per_step": int(S.x.nbytes * 2)},
+            "gpu_launches": 3,
+            "clocks": clk.summary(),
+            "roofline": None,
+            "cpu_baseline": cpu,
+            "counts": {"nonsingular": nonsing, "singular": sing,
+                       "failed": sum(not r.is_success() for r in rs), "codes": {c: codes.count(c) for c in set(codes)}},
+            "total_degree_same_system": {"paths": len(S2), "seconds": td_s, "nonsingular": nonsing2},
+            "speedup_vs_total_degree_gpu": td_s / (ms / 1000),
         }
         print(json.dumps(line), flush=True)
 

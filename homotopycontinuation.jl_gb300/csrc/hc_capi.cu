@@ -444,6 +444,7 @@ static int fail(hc_handle* h, int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+int hc_library_fail(int code, const char* msg) { return fail(nullptr, code, msg); }
 static int cuda_fail(hc_handle* h, cudaError_t e, const char* where) {
   return fail(h, HC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }

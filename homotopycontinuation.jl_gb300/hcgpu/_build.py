@@ -11,7 +11,7 @@ PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libhcgpu.so")
-SOURCES = ["hc_kernels.cu", "hc_capi.cu", "hc_peak.cu", "hc_mlp.cu", "hc_certify.cu"]
+SOURCES = ["hc_kernels.cu", "hc_capi.cu", "hc_peak.cu", "hc_mlp.cu", "hc_certify.cu", "hc_mixed.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "39"]
 

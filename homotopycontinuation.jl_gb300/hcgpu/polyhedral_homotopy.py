@@ -6,9 +6,10 @@ Solving F by the polyhedral method (Huber and Sturmfels 1995) takes three parts:
   MixedSubdivisions.jl (a dependency outside the reference tree, pinned by its compat entry
   "MixedSubdivisions 1"); :func:`fine_mixed_cells` restates the published method: a cell picks
   one edge {a_i, b_i} of every lifted support such that some inner normal (γ, 1) is minimised
-  on exactly that edge in every support. A depth-first search over the supports with a linear
-  feasibility test per partial choice finds all of them; the mixed volume is the sum of the
-  cells' volumes |det(a_i − b_i)|.
+  on exactly that edge in every support. hc_mixed_cells (csrc/hc_mixed.cu, host C++) finds all
+  of them by a depth-first search with a relation table of compatible edge pairs and a linear
+  feasibility test per partial choice; the mixed volume is the sum of the cells' volumes
+  |det(a_i − b_i)|.
 * the start solutions of every cell: a binomial system x^(a_i − b_i) = −c_{b_i}/c_{a_i}
   (src/binomial_system.jl), solved here through a Hermite normal form in logarithmic
   coordinates and refined there (:func:`solve_binomial`);
@@ -71,94 +72,41 @@ class MixedCell:
     volume: int
 
 
-def _lp_margin(Aeq, beq, Aub, bub, n):
-    """max s subject to Aeq γ = beq, Aub γ + s ≤ bub, s ≤ 1 (γ free); −inf if infeasible."""
-    from scipy.optimize import linprog
-
-    nv = n + 1
-    c = np.zeros(nv)
-    c[-1] = -1.0
-    A_ub = np.hstack([Aub, np.ones((Aub.shape[0], 1))]) if len(Aub) else None
-    A_eq = np.hstack([Aeq, np.zeros((Aeq.shape[0], 1))]) if len(Aeq) else None
-    bounds = [(None, None)] * n + [(None, 1.0)]
-    r = linprog(c, A_ub=A_ub, b_ub=bub if len(Aub) else None, A_eq=A_eq, b_eq=beq if len(Aeq) else None,
-                bounds=bounds, method="highs")
-    if r.status != 0:
-        return -math.inf
-    return -r.fun
-
-
-def _edge_rows(S, w, p, q):
-    """Constraints of 'edge {p, q} of the lifted support (S, w) is where (γ, 1) is minimal'."""
-    eq_row = (S[p] - S[q]).astype(np.float64)
-    eq_rhs = float(w[q] - w[p])
-    others = [c for c in range(len(S)) if c != p and c != q]
-    ub = (S[p][None, :] - S[others]).astype(np.float64) if others else np.zeros((0, S.shape[1]))
-    ub_rhs = (w[others] - w[p]).astype(np.float64) if others else np.zeros(0)
-    return eq_row, eq_rhs, ub, ub_rhs
-
-
 class _DegenerateLifting(Exception):
     pass
 
 
-def _mixed_cells_for_lifting(supports, lifting, tol):
+def _mixed_cells_native(supports, lifting):
+    """hc_mixed_cells (csrc/hc_mixed.cu): the lower-edge LPs, the relation table and the
+    depth-first search run in C++ on all host cores."""
+    L = _lib.load()
+    P = _lib.ptr
     n = supports[0].shape[1]
-    m = len(supports)
-    # lower edges of each lifted support
-    edges = []
-    for S, w in zip(supports, lifting):
-        E = []
-        for p in range(len(S)):
-            for q in range(p + 1, len(S)):
-                er, eb, U, ub = _edge_rows(S, w, p, q)
-                if not er.any():
-                    continue
-                if _lp_margin(er[None, :], np.array([eb]), U, ub, n) > tol:
-                    E.append((p, q, er, eb, U, ub))
-        edges.append(E)
-    order = sorted(range(m), key=lambda i: len(edges[i]))
-    cells = []
-    chosen = [None] * m
-
-    def rec(depth, Aeq, beq, Aub, bub):
-        if depth == m:
-            M = np.array(Aeq)
-            vol = int(round(abs(np.linalg.det(M))))
-            if vol == 0:
-                return
-            g = np.linalg.solve(M, np.array(beq))
-            # fine cell: every other lifted point lies strictly above the face
-            slack = np.array(bub) - np.array(Aub) @ g if len(Aub) else np.array([1.0])
-            eps = tol * max(1.0, np.abs(g).max())
-            if slack.min() < -eps:
-                return
-            if slack.min() <= eps:
-                raise _DegenerateLifting()
-            beta = np.array([float(supports[i][chosen[i][0]] @ g + lifting[i][chosen[i][0]]) for i in range(m)])
-            cells.append(MixedCell(indices=[tuple(chosen[i]) for i in range(m)], normal=g, beta=beta, volume=vol))
-            return
-        i = order[depth]
-        for (p, q, er, eb, U, ub) in edges[i]:
-            Aeq2 = Aeq + [er]
-            beq2 = beq + [eb]
-            Aub2 = Aub + list(U)
-            bub2 = bub + list(ub)
-            if depth + 1 < m:
-                if np.linalg.matrix_rank(np.array(Aeq2)) < len(Aeq2):
-                    continue
-                if _lp_margin(np.array(Aeq2), np.array(beq2), np.array(Aub2).reshape(-1, n), np.array(bub2), n) <= tol:
-                    continue
-            chosen[i] = (p, q)
-            rec(depth + 1, Aeq2, beq2, Aub2, bub2)
-            chosen[i] = None
-
-    rec(0, [], [], [], [])
-    return cells
+    nterms = np.array([len(S) for S in supports], dtype=np.int32)
+    pts = np.ascontiguousarray(np.concatenate(supports, axis=0), dtype=np.int32)
+    lif = np.ascontiguousarray(np.concatenate(lifting), dtype=np.int64)
+    cap = 1 << 14
+    while True:
+        idx = np.zeros((cap, 2 * n), dtype=np.int32)
+        nor = np.zeros((cap, n))
+        beta = np.zeros((cap, n))
+        vol = np.zeros(cap, dtype=np.int64)
+        cnt = np.zeros(1, dtype=np.int64)
+        rc = L.hc_mixed_cells(n, P(nterms), P(pts), P(lif), cap, P(idx), P(nor), P(beta), P(vol), P(cnt))
+        if rc == 6 and int(cnt[0]) > cap:  # HC_ERR_TOO_LARGE
+            cap = int(cnt[0])
+            continue
+        if rc == 1 and b"not generic" in (L.hc_last_error(None) or b""):
+            raise _DegenerateLifting()
+        _lib.check(rc)
+        break
+    k = int(cnt[0])
+    return [MixedCell(indices=[(int(idx[c, 2 * i]), int(idx[c, 2 * i + 1])) for i in range(n)], normal=nor[c].copy(),
+                      beta=beta[c].copy(), volume=int(vol[c])) for c in range(k)]
 
 
-def fine_mixed_cells(supports, lifting=None, seed: Optional[int] = None, max_lift: int = 2 ** 12, tol: float = 1e-7,
-                     max_tries: int = 8):
+def fine_mixed_cells(supports, lifting=None, seed: Optional[int] = None, max_lift: int = 2 ** 16,
+                     max_tries: int = 16):
     """(cells, lifting) of a fine mixed subdivision of the supports (list of terms × n integer
     arrays) under a random integer lifting (or the given one). A lifting that turns out
     non-generic is drawn again."""
@@ -168,7 +116,7 @@ def fine_mixed_cells(supports, lifting=None, seed: Optional[int] = None, max_lif
         lift = [np.asarray(w, dtype=np.int64) for w in lifting] if lifting is not None else \
             [rng.integers(0, max_lift, size=len(S)) for S in supports]
         try:
-            return _mixed_cells_for_lifting(supports, lift, tol), lift
+            return _mixed_cells_native(supports, lift), lift
         except _DegenerateLifting:
             if lifting is not None:
                 raise ValueError("the given lifting does not induce a fine mixed subdivision")

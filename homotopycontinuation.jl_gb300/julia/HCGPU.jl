@@ -270,4 +270,99 @@ function gpu_certify(F::HC.System, solutions::AbstractVector{<:AbstractVector})
     end
 end
 
+# options with some fields replaced (immutable struct: rebuilt field by field)
+function with_fields(o::HCOptions; kw...)
+    HCOptions(ntuple(i -> get(kw, fieldnames(HCOptions)[i], getfield(o, i)), fieldcount(HCOptions))...)
+end
+
+"""
+    gpu_polyhedral(F::System; only_non_zero = false)
+
+`solve(F; start_system = :polyhedral)` with both tracking stages on the GPU. The mixed cells,
+the lifting, the start coefficients and the start solutions are the reference's own
+(`polyhedral`, src/polyhedral.jl:197-408, which calls MixedSubdivisions.jl); the toric stage
+of `track(::PolyhedralTracker, …)` (src/polyhedral.jl:412-484) becomes two `hc_track_toric`
+calls over all paths (the second for the cells whose largest weight is ≥ 10, restarted with
+weights rescaled to a maximum of 10), and the coefficient homotopy one `hc_track`.
+"""
+function gpu_polyhedral(F::HC.System; only_non_zero = false)
+    PT, starts = HC.polyhedral(F; only_non_zero = only_non_zero)
+    H = PT.toric_tracker.homotopy
+    support, lifting = PT.support, PT.lifting
+    n = length(support)
+    # term tables in the order of the flattened supports (the order of H.weights)
+    eq = Int32[]; exps = Int32[]
+    for (i, A) in enumerate(support), k in 1:size(A, 2)
+        push!(eq, i - 1); append!(exps, Int32.(A[:, k]))
+    end
+    cfs(c) = reduce(vcat, [[real(z), imag(z)] for z in c])
+    ucf = cfs(H.system_coeffs)
+    pairs = collect(starts)                     # (cell, x) in the iterator's order
+    cells = unique(first.(pairs))
+    row = Dict(c => i - 1 for (i, c) in enumerate(cells))
+    nT = length(eq)
+    W1 = Float64[]; W2 = Float64[]; smax = Float64[]; smin2 = Float64[]
+    for c in cells
+        _, s_max = HC.update_weights!(H, support, lifting, c; min_weight = 1.0)
+        append!(W1, H.weights); push!(smax, s_max)
+        s_min, _ = HC.update_weights!(H, support, lifting, c; max_weight = 10.0)
+        append!(W2, H.weights); push!(smin2, s_min)
+    end
+    m = length(pairs)
+    rows = Int32[row[p[1]] for p in pairs]
+    S = flat_starts(last.(pairs), n)
+    tend = [smax[r+1] < 10 ? 1.0 : clamp(0.1^(10 / smax[r+1]), 0.9, 1 - 1e-6) for r in rows]
+    res = Vector{HCPathResult}(undef, m)
+    sol = Vector{Float64}(undef, 2n * m)
+    o = default_options(precision = 0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hc_create, libhcgpu), Cint, (Ref{HCOptions}, Ref{Ptr{Cvoid}}),
+                Ref(with_fields(o; max_initial_step_size = 0.2)), h))
+    try
+        settoric(W) = check(ccall((:hc_set_toric, libhcgpu), Cint,
+                                  (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Float64}),
+                                  h[], n, nT, eq, exps, ucf, length(cells), W), h[])
+        track(k, X, t1, t0, ω, μ, R, Xo) = check(ccall((:hc_track_toric, libhcgpu), Cint,
+            (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+             Ptr{Float64}, Ptr{HCPathResult}, Ptr{Float64}),
+            h[], k, X, rows[idx_cur[]], t1, t0, ω, μ, R, Xo), h[])
+        idx_cur = Ref(collect(1:m))
+        settoric(W1)
+        track(m, S, zeros(m), tend, fill(20.0, m), fill(1e-12, m), res, sol)
+        # restart (src/polyhedral.jl:455-484): TrackerCode success == 1
+        idx = [k for k in 1:m if tend[k] < 1 && res[k].return_code == 1]
+        if !isempty(idx)
+            check(ccall((:hc_set_options, libhcgpu), Cint, (Ptr{Cvoid}, Ref{HCOptions}), h[],
+                        Ref(with_fields(o; min_step_size = 0.0))), h[])
+            settoric(W2)
+            idx_cur[] = idx
+            X = reduce(vcat, [sol[2n*(k-1)+1:2n*k] for k in idx])
+            tr = [tend[k]^(1 / smin2[rows[k]+1]) for k in idx]
+            R2 = Vector{HCPathResult}(undef, length(idx)); X2 = similar(X)
+            track(length(idx), X, tr, ones(length(idx)), [res[k].omega for k in idx], [res[k].mu for k in idx],
+                  R2, X2)
+            for (j, k) in enumerate(idx)
+                res[k] = R2[j]; sol[2n*(k-1)+1:2n*k] = X2[2n*(j-1)+1:2n*j]
+            end
+        end
+        # coefficient homotopy t·F(x; start) + (1 − t)·F(x; target) with the endgame
+        tcf = cfs(reduce(vcat, PT.generic_tracker.tracker.homotopy.target_coeffs))
+        ok = [k for k in 1:m if res[k].return_code == 1]
+        check(ccall((:hc_set_options, libhcgpu), Cint, (Ptr{Cvoid}, Ref{HCOptions}), h[], Ref(o)), h[])
+        check(ccall((:hc_set_homotopy, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Int32},
+                     Ptr{Int32}, Ptr{Float64}, Float64, Float64),
+                    h[], n, nT, eq, exps, ucf, nT, eq, exps, tcf, 1.0, 0.0), h[])
+        X = reduce(vcat, [sol[2n*(k-1)+1:2n*k] for k in ok]; init = Float64[])
+        R3 = Vector{HCPathResult}(undef, length(ok)); X3 = similar(X)
+        check(ccall((:hc_track, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Int64, Ptr{Float64}, Cint, Float64, Float64, Float64, Float64,
+                     Ptr{HCPathResult}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                    h[], length(ok), X, 1, 1.0, 0.0, 0.0, 0.0, R3, X3, C_NULL, C_NULL), h[])
+        to_result(R3, X3, 0, 0, n, [last(pairs[k]) for k in ok])
+    finally
+        ccall((:hc_destroy, libhcgpu), Cvoid, (Ptr{Cvoid},), h[])
+    end
+end
+
 end # module

@@ -146,6 +146,19 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
                    const double* t0, const double* omega, const double* mu, hc_path_result* out_results,
                    double* out_solutions);
 
+/* Fine mixed cells of n supports under an integer lifting (host code, no GPU): the start
+ * cells of the polyhedral homotopy, which the reference takes from MixedSubdivisions.jl
+ * (fine_mixed_cells, called at src/polyhedral.jl:23). Support i has nterms[i] points; points
+ * holds all supports' points (Σ nterms × n, row-major), lifting one integer per point. For
+ * every cell (at most max_cells; *out_ncells receives the count, HC_ERR_TOO_LARGE when it
+ * exceeds max_cells) out_indices holds the two point indices per support (max_cells × 2n),
+ * out_normals the inner normal γ, out_beta β_i = min over support i of ⟨a, γ⟩ + ω(a)
+ * (max_cells × n each) and out_volumes |det(a_i − b_i)|. A lifting that does not induce a fine
+ * subdivision returns HC_ERR_INVALID_ARG ("not generic"); draw another. */
+int hc_mixed_cells(int n, const int32_t* nterms, const int32_t* points, const int64_t* lifting, int64_t max_cells,
+                   int32_t* out_indices, double* out_normals, double* out_beta, int64_t* out_volumes,
+                   int64_t* out_ncells);
+
 /* Request cancellation of a running hc_track on this handle (thread-safe). Paths not yet
  * finished report TrackerCode terminated_unknown and hc_track returns HC_ERR_CANCELLED. */
 int hc_cancel(hc_handle* h);

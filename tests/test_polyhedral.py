@@ -51,6 +51,15 @@ def test_cyclic5_kat():
         assert np.abs(F.evaluate(r.solution)).max() < 1e-10
 
 
+def test_cyclic7_kat():
+    # test/polyhedral_test.jl:43-46: 924 solutions of cyclic-7
+    F = hc.cyclic(7)
+    T, S = ph.polyhedral(F, seed=6)
+    assert len(S) == 924
+    rs = T.track_arrays(S)
+    assert sum(r.is_success() for r in rs) == 924
+
+
 def test_solve_polyhedral_affine_sqr():
     # test/solve_test.jl:95-100: 2 solutions
     x, y = hc.variables(2)

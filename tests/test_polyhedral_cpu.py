@@ -45,9 +45,9 @@ def test_only_torus_kat():
     assert ph.paths_to_track(F, only_torus=True) == 54
 
 
-@pytest.mark.parametrize("n,mv", [(5, 70), (6, 156)])
+@pytest.mark.parametrize("n,mv", [(5, 70), (6, 156), (7, 924), (8, 2560)])
 def test_cyclic_mixed_volume(n, mv):
-    # cyclic-5: 70 (test/polyhedral_test.jl:39-41); cyclic-6: 156
+    # cyclic-5: 70, cyclic-7: 924 (test/polyhedral_test.jl:39-46); cyclic-6: 156, cyclic-8: 2560
     assert ph.mixed_volume(hc.cyclic(n)) == mv
 
 
