@@ -513,7 +513,9 @@ def main_uneven(args, torch, hc, _lib, local):
 def main_polyhedral(args, torch, hc, _lib, local):
     """solve(F; start_system = :polyhedral) of the 8x8 sparse system: mixed cells and start
     solutions on the host (timed apart), then per step both tracking stages through the host
-    API (hc_track_toric, hc_track), with the total-degree solve of the same system beside it."""
+    API (hc_track_toric, then hc_track for the coefficient homotopy with the endgame), in FP64
+    with the plain step rule; the coefficient stage with --precision / --step-control and the
+    total-degree solve of the same system are reported beside it."""
     from hcgpu import polyhedral_homotopy as ph
 
     rank = int(os.environ.get("RANK", "0"))
@@ -521,24 +523,38 @@ def main_polyhedral(args, torch, hc, _lib, local):
         raise SystemExit("--workload polyhedral runs on one GPU")
     F, g = hc.sparse_random_system(8, 8, 4, seed=args.seed)
     t = time.perf_counter()
-    T, S = ph.polyhedral(F, seed=args.seed + 1)
+    T64, S = ph.polyhedral(F, seed=args.seed + 1)
     prep_s = time.perf_counter() - t
     npaths = len(S)
-    for _ in range(args.warmup):
-        T.track_arrays(S)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        times = []
-        for _ in range(args.steps):
+    T = ph.PolyhedralTracker(T64.supports, T64.start_coeffs, T64.target_coeffs, T64.lifting, T64.cells, T64.n,
+                             hc.TrackerOptions(precision=args.precision, step_control=args.step_control))
+
+    def timed(Tr, steps, warmup):
+        for _ in range(warmup):
+            Tr.track_arrays(S)
+        out = []
+        for _ in range(steps):
             torch.cuda.synchronize()
-            t = time.perf_counter()
-            rs = T.track_arrays(S)
-            times.append(time.perf_counter() - t)
+            t0 = time.perf_counter()
+            rs_ = Tr.track_arrays(S)
+            out.append(time.perf_counter() - t0)
+        return out, rs_
+
+    with ClockSampler(local) as clk:
+        times, rs64 = timed(T64, args.steps, args.warmup)
     ms = 1000 * float(np.mean(times))
-    codes = [r.return_code for r in rs]
-    nonsing = sum(r.is_success() and not r.is_singular() for r in rs)
-    sing = sum(r.is_success() and r.is_singular() for r in rs)
-    # total degree on the same system (plain FP64, same options)
+    talt, rs = timed(T, 1, 1)
+
+    def counts(rr):
+        return {"nonsingular": sum(r.is_success() and not r.is_singular() for r in rr),
+                "singular": sum(r.is_success() and r.is_singular() for r in rr),
+                "failed": sum(not r.is_success() for r in rr)}
+
+    err = 0.0
+    for a_, b_ in zip(rs, rs64):
+        if a_.is_success() and b_.is_success() and not a_.is_singular() and not b_.is_singular():
+            err = max(err, float(np.abs(a_.solution - b_.solution).max() / max(np.abs(b_.solution).max(), 1e-300)))
+    # total degree on the same system (plain FP64)
     H = hc.total_degree_homotopy(F, g)
     S2 = hc.total_degree_start_solutions(H.degrees)
     E = hc.EndgameTracker(H, hc.TrackerOptions())
@@ -547,7 +563,6 @@ def main_polyhedral(args, torch, hc, _lib, local):
     t = time.perf_counter()
     r2 = E.track_batch(S2)
     td_s = time.perf_counter() - t
-    nonsing2 = sum(r.is_success() and not r.is_singular() for r in r2)
     # CPU baseline: the oracle's polyhedral tracker on an evenly spaced sample of the paths
     cpu = None
     if not args.no_cpu:
@@ -560,13 +575,15 @@ def main_polyhedral(args, torch, hc, _lib, local):
                                           cell_of=S.cell_of[idx], x=S.x[idx])
         cores = os.cpu_count()
         t = time.perf_counter()
-        ocodes, ox, _ = po.track(T, sub, nthreads=cores)
+        ocodes, ox, _ = po.track(T64, sub, nthreads=cores)
         dt = time.perf_counter() - t
-        agree = int(sum((ocodes[j] == 1) == rs[k].is_success() for j, k in enumerate(idx)))
+        agree = int(sum((ocodes[j] == 1) == rs64[k].is_success() for j, k in enumerate(idx)))
         cpu = {"value": sample / dt, "unit": "paths/s", "cores": cores, "kind": "port",
                "sample": f"{sample} of {npaths} paths (evenly spaced), C++ FP64 restatement of the reference "
-                         f"PolyhedralTracker on {cores} threads, {dt:.1f} s; success flags agree on {agree}"}
+                         f"PolyhedralTracker on {cores} threads, {dt:.1f} s; success flags agree with the FP64 GPU "
+                         f"run on {agree}"}
     if rank == 0:
+        codes = [r.return_code for r in rs64]
         line = {
             "metric": METRIC, "value": npaths / (ms / 1000), "unit": "paths/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -582,9 +599,12 @@ def main_polyhedral(args, torch, hc, _lib, local):
             "clocks": clk.summary(),
             "roofline": None,
             "cpu_baseline": cpu,
-            "counts": {"nonsingular": nonsing, "singular": sing,
-                       "failed": sum(not r.is_success() for r in rs), "codes": {c: codes.count(c) for c in set(codes)}},
-            "total_degree_same_system": {"paths": len(S2), "seconds": td_s, "nonsingular": nonsing2},
+            "counts": counts(rs64), "codes": {c: codes.count(c) for c in set(codes)},
+            f"coefficient_stage_{args.precision}_{args.step_control}": {
+                "value": npaths / float(np.mean(talt)), "unit": "paths/s", "counts": counts(rs),
+                "counts_identical_to_fp64": counts(rs) == counts(rs64), "max_rel_endpoint_err_vs_fp64": err},
+            "total_degree_same_system": {"paths": len(S2), "seconds": td_s,
+                                         "nonsingular": sum(r.is_success() and not r.is_singular() for r in r2)},
             "speedup_vs_total_degree_gpu": td_s / (ms / 1000),
         }
         print(json.dumps(line), flush=True)

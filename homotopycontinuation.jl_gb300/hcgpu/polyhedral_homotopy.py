@@ -342,8 +342,11 @@ class PolyhedralTracker:
         self.W2 = np.array(W2).reshape(len(cells), -1)
         self.wmax = wmax
         self._last_toric = None
+        self._handles = {}  # toric handles (stage 1, restart) and the endgame tracker, made once
 
-    def _toric_handle(self, W, options):
+    def _toric_handle(self, W, options, key=None):
+        if key is not None and key in self._handles:
+            return self._handles[key]
         h = _Handle(options)
         eq, ex, cf = self.generic_start.term_arrays()
         P = _lib.ptr
@@ -351,6 +354,8 @@ class PolyhedralTracker:
         W = np.ascontiguousarray(W, dtype=np.float64)
         _lib.check(h.L.hc_set_toric(h.h, self.n, len(eq), P(eq), P(ex), P(cf), W.shape[0], P(W)), h.h)
         h.n = self.n
+        if key is not None:
+            self._handles[key] = h
         return h
 
     def _toric_track(self, h, x, rows, t1, t0, omega=None, mu=None):
@@ -377,7 +382,7 @@ class PolyhedralTracker:
         t_end = np.where(split, np.clip(0.1 ** (10.0 / np.where(split, smax, 1.0)), 0.9, 1 - 1e-6), 1.0)
         o1 = make_options(to, None)
         o1.max_initial_step_size = 0.2
-        h1 = self._toric_handle(self.W1, o1)
+        h1 = self._toric_handle(self.W1, o1, "toric")
         res, sol = self._toric_track(h1, x, rows, np.zeros(npaths), t_end, np.full(npaths, 20.0),
                                      np.full(npaths, 1e-12))
         codes = res["return_code"].copy()
@@ -390,7 +395,7 @@ class PolyhedralTracker:
         if len(idx):
             o2 = make_options(to, None)
             o2.min_step_size = 0.0
-            h2 = self._toric_handle(self.W2, o2)
+            h2 = self._toric_handle(self.W2, o2, "restart")
             smin2 = np.array([self.wmax[c][1] for c in rows[idx]])
             t_restart = t_end[idx] ** (1.0 / smin2)
             r2, s2 = self._toric_track(h2, sol[idx], rows[idx], t_restart, np.ones(len(idx)), omega[idx], mu[idx])
@@ -409,7 +414,9 @@ class PolyhedralTracker:
         ok = codes == _TRACKER_SUCCESS
         H = TotalDegreeHomotopy(F=self.target, G=self.generic_start, gamma=1.0 + 0j, degrees=self.target.degrees(),
                                 scaling=np.ones(self.n))
-        E = EndgameTracker(H, self.tracker_options, self.endgame_options)
+        E = self._handles.get("generic")
+        if E is None:
+            E = self._handles["generic"] = EndgameTracker(H, self.tracker_options, self.endgame_options)
         out: List[Optional[PathResult]] = [None] * len(x1)
         idx = np.nonzero(ok)[0]
         if len(idx):
