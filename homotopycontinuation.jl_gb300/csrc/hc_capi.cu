@@ -55,7 +55,7 @@ struct HostProg {
   std::vector<float2> vcoef32;
   std::vector<uint16_t> vmono;
   std::vector<uint32_t> jcode;
-  std::vector<int> vorig;  // value term k of the program is the caller's term vorig[k] (F, then G)
+  std::vector<int> vorig;  // value storage index k holds the caller's term vorig[k] (F, then G)
   // operation census for the flop model
   long long val_terms = 0, jac_terms = 0;
 };
@@ -84,22 +84,89 @@ struct MonoTable {
   }
 };
 
-// Cut rows (terms sorted by row, then by multiplier) into segments of one multiplier and at
-// most ~T/(32*per_lane) terms, and spread them over the 32 lanes (longest first to the least
-// loaded lane). Slots are numbered row-major so a row's partials are contiguous.
-void build_segments(int nrows, const std::vector<Term>& terms, int per_lane, HostProg::Rows& R) {
+// Lane schedule of a row table (terms sorted by row, then by multiplier), in two parts.
+//  * Aligned groups: rows with identical (monomial, multiplier) sequences — every F row of a
+//    dense system, and for each variable the n rows ∂F_i/∂x_j — are run g = group size lanes
+//    side by side: lane set k (of s = ⌊32/g⌋ sets) takes piece k of every such row, so the g
+//    lanes of a set read the same monomial at every step (one broadcast shared-memory load)
+//    and the pieces are equal.
+//  * The other rows are cut into segments of one multiplier and at most ~T/(32·per_lane) terms
+//    and spread over the lanes, longest first to the least loaded lane.
+// Slots are numbered row-major so a row's partials are contiguous and its total is a
+// fixed-order sum; a lane runs its aligned pieces first, in the same order as its set.
+// Storage: an aligned piece of the g rows is stored position-major (the g rows' terms at one
+// position side by side), so the set's lanes read g consecutive coefficients; a segment is
+// (stride, first storage index, end index, slot | multiplier << 24), and pos[k] receives the
+// storage index of term k.
+void build_segments(int nrows, const std::vector<Term>& terms, int per_lane, HostProg::Rows& R,
+                    std::vector<int>& pos, bool align) {
   R.nrows = nrows;
   int T = (int)terms.size();
   std::vector<int> row_begin(nrows + 1, 0);
   for (int k = 0; k < T; ++k) row_begin[terms[k].row + 1] += 1;
   for (int r = 0; r < nrows; ++r) row_begin[r + 1] += row_begin[r];
-  int L = std::max(8, (T + 32 * per_lane - 1) / (32 * per_lane));
   struct Chunk {
-    int row, b, e, slot, mult;
+    int row, b, e, mult, start, stride;  // terms [b, e) stored from start with the stride
   };
   std::vector<Chunk> chunks;
-  R.row_slot.assign(nrows + 1, 0);
+  std::vector<std::vector<int>> lane_chunks(32);
+  pos.assign(T, 0);
+  int next = 0;  // next free storage index
+  std::vector<long long> load(32, 0);
+  // rows grouped by their (monomial, multiplier) sequence
+  std::map<std::vector<std::pair<int, int>>, std::vector<int>> groups;
+  for (int r = 0; r < nrows && align; ++r) {
+    if (row_begin[r + 1] - row_begin[r] < 8) continue;
+    std::vector<std::pair<int, int>> sig;
+    for (int k = row_begin[r]; k < row_begin[r + 1]; ++k) sig.push_back({terms[k].mono, terms[k].mult});
+    groups[sig].push_back(r);
+  }
+  // the group size carrying the most terms
+  std::map<int, long long> by_size;
+  for (auto& kv : groups)
+    if (kv.second.size() >= 2) by_size[(int)kv.second.size()] += (long long)kv.first.size() * kv.second.size();
+  int g = 0;
+  long long best = 0;
+  for (auto& kv : by_size)
+    if (kv.first <= 32 && kv.second > best) {
+      best = kv.second;
+      g = kv.first;
+    }
+  std::vector<char> aligned(nrows, 0);
+  if (g >= 2) {
+    const int sets = 32 / g;
+    for (auto& kv : groups) {
+      if ((int)kv.second.size() != g) continue;
+      const int Lr = (int)kv.first.size();
+      for (int set = 0; set < sets; ++set) {
+        const int pb = (int)((long long)Lr * set / sets), pe = (int)((long long)Lr * (set + 1) / sets);
+        // the piece, cut where the multiplier changes (the same places in every row of the group)
+        int k = pb;
+        while (k < pe) {
+          int k2 = k;
+          while (k2 < pe && kv.first[k2].second == kv.first[k].second) ++k2;
+          for (int m = 0; m < g; ++m) {
+            const int r = kv.second[m], lane = set * g + m;
+            lane_chunks[lane].push_back((int)chunks.size());
+            chunks.push_back({r, row_begin[r] + k, row_begin[r] + k2, kv.first[k].second, next + m, g});
+            for (int q = k; q < k2; ++q) pos[row_begin[r] + q] = next + (q - k) * g + m;
+            load[lane] += k2 - k + 2;
+          }
+          next += (k2 - k) * g;
+          k = k2;
+        }
+      }
+      for (int r : kv.second) aligned[r] = 1;
+    }
+  }
+  // the remaining rows
+  int Trest = 0;
+  for (int r = 0; r < nrows; ++r)
+    if (!aligned[r]) Trest += row_begin[r + 1] - row_begin[r];
+  const int L = std::max(8, (Trest + 32 * per_lane - 1) / (32 * per_lane));
+  std::vector<int> rest;
   for (int r = 0; r < nrows; ++r) {
+    if (aligned[r]) continue;
     int b = row_begin[r], e = row_begin[r + 1];
     int k = b;
     while (k < e) {  // runs of equal multiplier
@@ -109,34 +176,50 @@ void build_segments(int nrows, const std::vector<Term>& terms, int per_lane, Hos
       int nc = (t + L - 1) / L;
       for (int c = 0; c < nc; ++c) {
         int cb = k + (int)((long long)t * c / nc), ce = k + (int)((long long)t * (c + 1) / nc);
-        chunks.push_back({r, cb, ce, (int)chunks.size(), terms[k].mult});
+        rest.push_back((int)chunks.size());
+        chunks.push_back({r, cb, ce, terms[k].mult, next, 1});
+        for (int q = cb; q < ce; ++q) pos[q] = next + (q - cb);
+        next += ce - cb;
       }
       k = k2;
     }
-    R.row_slot[r + 1] = (int)chunks.size();
   }
-  R.nslots = (int)chunks.size();
-  std::vector<int> order(chunks.size());
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+  std::stable_sort(rest.begin(), rest.end(), [&](int a, int b) {
     return (chunks[a].e - chunks[a].b) > (chunks[b].e - chunks[b].b);
   });
-  std::vector<long long> load(32, 0);
-  std::vector<std::vector<int>> lane_chunks(32);
-  for (int ci : order) {
-    int best = 0;
+  for (int ci : rest) {
+    int bl = 0;
     for (int l = 1; l < 32; ++l)
-      if (load[l] < load[best]) best = l;
-    load[best] += chunks[ci].e - chunks[ci].b + 2;
-    lane_chunks[best].push_back(ci);
+      if (load[l] < load[bl]) bl = l;
+    load[bl] += chunks[ci].e - chunks[ci].b + 2;
+    lane_chunks[bl].push_back(ci);
   }
+  for (int l = 0; l < 32; ++l) {  // aligned pieces first (in set order), then the rest by position
+    auto it = std::stable_partition(lane_chunks[l].begin(), lane_chunks[l].end(),
+                                    [&](int ci) { return aligned[chunks[ci].row] != 0; });
+    std::sort(it, lane_chunks[l].end());
+  }
+  // slots in row-major order
+  std::vector<int> order(chunks.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    return chunks[a].row != chunks[b].row ? chunks[a].row < chunks[b].row : chunks[a].b < chunks[b].b;
+  });
+  std::vector<int> slot(chunks.size());
+  R.row_slot.assign(nrows + 1, 0);
+  for (size_t i = 0; i < order.size(); ++i) {
+    slot[order[i]] = (int)i;
+    R.row_slot[chunks[order[i]].row + 1] += 1;
+  }
+  for (int r = 0; r < nrows; ++r) R.row_slot[r + 1] += R.row_slot[r];
+  R.nslots = (int)chunks.size();
   R.seg.clear();
   R.lane_seg.assign(33, 0);
   for (int l = 0; l < 32; ++l) {
-    std::sort(lane_chunks[l].begin(), lane_chunks[l].end());
-    for (int ci : lane_chunks[l])
-      R.seg.push_back(make_int4(chunks[ci].row, chunks[ci].b, chunks[ci].e,
-                                chunks[ci].slot | (chunks[ci].mult << 24)));
+    for (int ci : lane_chunks[l]) {
+      const Chunk& c = chunks[ci];
+      R.seg.push_back(make_int4(c.stride, c.start, c.start + (c.e - c.b) * c.stride, slot[ci] | (c.mult << 24)));
+    }
     R.lane_seg[l + 1] = (int)R.seg.size();
   }
 }
@@ -226,17 +309,22 @@ int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, con
   addv(nF, F_eq, F_exps, F_coef, 0);
   addv(nG, G_eq, G_exps, G_coef, n);
   std::stable_sort(vt.begin(), vt.end(), [](const Term& a, const Term& b) { return a.row < b.row; });
+  // value terms at their storage indices (build_segments)
+  std::vector<int> posv, posj;
+  build_segments(2 * n, vt, 2, P.val, posv, true);
   P.vcoef64.resize(vt.size());
   P.vcoef32.resize(vt.size());
   P.vmono.resize(vt.size());
   P.vorig.resize(vt.size());
   for (size_t k = 0; k < vt.size(); ++k) {
-    P.vorig[k] = vt[k].orig;
-    P.vcoef64[k] = make_double2(vt[k].re, vt[k].im);
-    P.vcoef32[k] = make_float2((float)vt[k].re, (float)vt[k].im);
-    P.vmono[k] = (uint16_t)vt[k].mono;
+    const int p = posv[k];
+    P.vorig[p] = vt[k].orig;
+    P.vcoef64[p] = make_double2(vt[k].re, vt[k].im);
+    P.vcoef32[p] = make_float2((float)vt[k].re, (float)vt[k].im);
+    P.vmono[p] = (uint16_t)vt[k].mono;
   }
-  // Jacobian terms: ∂/∂x_j of value term k → (row, monomial e - e_j, value term k, e_j)
+  // Jacobian terms: ∂/∂x_j of value term k → (row, monomial e - e_j, storage index of value
+  // term k, e_j)
   std::vector<Term> jt;
   for (size_t k = 0; k < vt.size(); ++k) {
     const std::vector<int>& ex = vexp[vt[k].orig];
@@ -246,18 +334,17 @@ int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, con
       if (ex[j] > 0) {
         std::vector<int> d = ex;
         d[j] -= 1;
-        jt.push_back({off + j * n + eq, index[d], 0, 0, (int)k, ex[j], 0});
+        jt.push_back({off + j * n + eq, index[d], 0, 0, posv[k], ex[j], 0});
       }
   }
   std::stable_sort(jt.begin(), jt.end(), [](const Term& a, const Term& b) {
     return a.row != b.row ? a.row < b.row : a.mult < b.mult;
   });
+  build_segments(2 * n * n, jt, 4, P.jac, posj, false);
   P.jcode.resize(jt.size());
-  for (size_t k = 0; k < jt.size(); ++k) P.jcode[k] = (uint32_t)jt[k].mono | ((uint32_t)jt[k].vterm << 16);
+  for (size_t k = 0; k < jt.size(); ++k) P.jcode[posj[k]] = (uint32_t)jt[k].mono | ((uint32_t)jt[k].vterm << 16);
   P.val_terms = (long long)vt.size();
   P.jac_terms = (long long)jt.size();
-  build_segments(2 * n, vt, 2, P.val);
-  build_segments(2 * n * n, jt, 4, P.jac);
   return HC_OK;
 }
 

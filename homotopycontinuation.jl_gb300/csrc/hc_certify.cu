@@ -102,7 +102,7 @@ __device__ void rows_balls(const DevProg& P, const DevRows& R, bool jac, const c
     int4 g = R.seg[s];
     cb acc = cb_point(C64(0.0));
     const int mult = (g.w >> 24) & 0xff;
-    for (int t = g.y; t < g.z; ++t) {
+    for (int t = g.y; t < g.z; t += g.x) {
       int m, vt;
       if (jac) {
         uint32_t code = P.jcode[t];

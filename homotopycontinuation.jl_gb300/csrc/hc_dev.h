@@ -21,7 +21,7 @@ namespace hcd {
 
 struct DevRows {
   int nrows, nterms, nslots, nseg;
-  const int4* seg;      // [nseg] (row, term begin, term end, slot), grouped by lane
+  const int4* seg;      // [nseg] (stride, term begin, term end, slot | mult << 24), grouped by lane
   const int* lane_seg;  // [33]
   const int* row_slot;  // [nrows + 1]
 };

@@ -455,16 +455,17 @@ struct PathTracker {
     for (int s = s0; s < s1e; ++s) {
       int4 g = __ldg(R.seg + s);
       c64 a0 = C64(0.0), a1 = a0, a2 = a0, a3 = a0;
+      const int D = g.x;  // the segment's stride between consecutive terms
       int t = g.y;
-      for (; t + 4 <= g.z; t += 4) {
-        int m0 = vmono[t], m1 = vmono[t + 1], m2 = vmono[t + 2], m3 = vmono[t + 3];
-        c64 c0 = vc[t], c1 = vc[t + 1], c2 = vc[t + 2], c3 = vc[t + 3];
+      for (; t + 3 * D < g.z; t += 4 * D) {
+        int m0 = vmono[t], m1 = vmono[t + D], m2 = vmono[t + 2 * D], m3 = vmono[t + 3 * D];
+        c64 c0 = vc[t], c1 = vc[t + D], c2 = vc[t + 2 * D], c3 = vc[t + 3 * D];
         a0 = cfma(c0, mono64[m0], a0);
         a1 = cfma(c1, mono64[m1], a1);
         a2 = cfma(c2, mono64[m2], a2);
         a3 = cfma(c3, mono64[m3], a3);
       }
-      for (; t < g.z; ++t) a0 = cfma(vc[t], mono64[vmono[t]], a0);
+      for (; t < g.z; t += D) a0 = cfma(vc[t], mono64[vmono[t]], a0);
       pp[g.w & 0xffffff] = (a0 + a1) + (a2 + a3);
     }
     __syncwarp();
@@ -497,15 +498,16 @@ struct PathTracker {
       T a0, a1, a2, a3;
       a0.re = a0.im = 0;
       a1 = a2 = a3 = a0;
+      const int D = g.x;
       int t = g.y;
-      for (; t + 4 <= g.z; t += 4) {
-        uint32_t k0 = jcode[t], k1 = jcode[t + 1], k2 = jcode[t + 2], k3 = jcode[t + 3];
+      for (; t + 3 * D < g.z; t += 4 * D) {
+        uint32_t k0 = jcode[t], k1 = jcode[t + D], k2 = jcode[t + 2 * D], k3 = jcode[t + 3 * D];
         a0 = cfma(cf[k0 >> 16], mv[k0 & 0xffff], a0);
         a1 = cfma(cf[k1 >> 16], mv[k1 & 0xffff], a1);
         a2 = cfma(cf[k2 >> 16], mv[k2 & 0xffff], a2);
         a3 = cfma(cf[k3 >> 16], mv[k3 & 0xffff], a3);
       }
-      for (; t < g.z; ++t) {
+      for (; t < g.z; t += D) {
         uint32_t k0 = jcode[t];
         a0 = cfma(cf[k0 >> 16], mv[k0 & 0xffff], a0);
       }
@@ -585,7 +587,7 @@ struct PathTracker {
     for (int s = s0; s < s1e; ++s) {
       int4 g = __ldg(R.seg + s);
       cdd acc = cdd_of(C64(0.0));
-      for (int tt = g.y; tt < g.z; ++tt) acc = acc + cdd_of(vc[tt]) * md[vmono[tt]];
+      for (int tt = g.y; tt < g.z; tt += g.x) acc = acc + cdd_of(vc[tt]) * md[vmono[tt]];
       pp[g.w & 0xffffff] = acc;
     }
     __syncwarp();
@@ -635,7 +637,7 @@ struct PathTracker {
     for (int s = s0; s < s1e; ++s) {
       int4 g = __ldg(R.seg + s);
       c64 acc = C64(0.0);
-      for (int k = g.y; k < g.z; ++k) {
+      for (int k = g.y; k < g.z; k += g.x) {
         const c64* Sm = S + (int)vmono[k] * 4;
         const double w = tw[k];
         const c64 u0 = vcoef64[k];
@@ -756,10 +758,11 @@ struct PathTracker {
       a0.re = a0.im = 0;
       a1 = b0 = b1 = a0;
       float e0 = 0.f, e1 = 0.f;
+      const int D = g.x;
       int tt = g.y;
-      for (; tt + 2 <= g.z; tt += 2) {
-        int m0 = vmono[tt], m1 = vmono[tt + 1];
-        T c0 = cf[tt], c1 = cf[tt + 1];
+      for (; tt + D < g.z; tt += 2 * D) {
+        int m0 = vmono[tt], m1 = vmono[tt + D];
+        T c0 = cf[tt], c1 = cf[tt + D];
         const T* q0 = (m0 < top) ? S + m0 * 4 + lo : ST + (m0 - top) * 2;
         const T* q1 = (m1 < top) ? S + m1 * 4 + lo : ST + (m1 - top) * 2;
         int d0 = (m0 < top) ? hi - lo : 1, d1 = (m1 < top) ? hi - lo : 1;
@@ -774,7 +777,7 @@ struct PathTracker {
           e1 += ac0 * (fabsf(v01.re) + fabsf(v01.im)) + ac1 * (fabsf(v11.re) + fabsf(v11.im));
         }
       }
-      for (; tt < g.z; ++tt) {
+      for (; tt < g.z; tt += D) {
         int m0 = vmono[tt];
         T c0 = cf[tt];
         const T* q0 = (m0 < top) ? S + m0 * 4 + lo : ST + (m0 - top) * 2;
