@@ -265,6 +265,8 @@ def cell_weights(supports, lifting, cell: MixedCell, min_weight=None, max_weight
                 s_max = max(s_max, s)
                 s_min = min(s_min, s)
     w = np.array(ws)
+    if not math.isfinite(s_min):  # binomial supports only: no term besides the cell's
+        return w, (min_weight if min_weight is not None else 1.0), 0.0
     if min_weight is not None:
         lam = s_min / min_weight
         w = w / lam

@@ -60,6 +60,26 @@ def test_cyclic7_kat():
     assert sum(r.is_success() for r in rs) == 924
 
 
+def test_univariate_and_zero_solutions():
+    x, = hc.variables(1)
+    F = hc.System.from_polys([x ** 5 - 3 * x ** 2 + 1])
+    R = hc.solve(F, start_system="polyhedral", seed=1)
+    assert R.nsolutions() == 5
+    roots = np.roots([1, 0, 0, -3, 0, 1])
+    for r in R.path_results:
+        assert np.abs(roots - r.solution[0]).min() < 1e-10
+    # y^2 + z = z^3 - y = 0: five solutions in the torus and (0, 0)
+    y, z = hc.variables(2)
+    H = hc.System.from_polys([y ** 2 + z, z ** 3 - y])
+    T, S = ph.polyhedral(H, seed=2)
+    assert len(S) == 6
+    sols = [r.solution for r in T.track_arrays(S) if r.is_success()]
+    assert len(sols) == 6
+    assert min(np.abs(s).max() for s in sols) < 1e-10
+    T, S = ph.polyhedral(H, only_non_zero=True, seed=2)
+    assert sum(r.is_success() for r in T.track_arrays(S)) == 5
+
+
 def test_solve_polyhedral_affine_sqr():
     # test/solve_test.jl:95-100: 2 solutions
     x, y = hc.variables(2)

@@ -51,6 +51,18 @@ def test_cyclic_mixed_volume(n, mv):
     assert ph.mixed_volume(hc.cyclic(n)) == mv
 
 
+def test_small_systems_by_hand():
+    # x^5 - 3x^2 + 1: 5 roots; y z = 1, y + z = 3: 2; y^2 + z = z^3 - y = 0: z = -y^2 and
+    # y (y^5 + 1) = 0, so 5 solutions in the torus and (0, 0) besides
+    x, = hc.variables(1)
+    assert ph.mixed_volume(hc.System.from_polys([x ** 5 - 3 * x ** 2 + 1])) == 5
+    y, z = hc.variables(2)
+    assert ph.mixed_volume(hc.System.from_polys([y * z - 1, y + z - 3])) == 2
+    H = hc.System.from_polys([y ** 2 + z, z ** 3 - y])
+    assert ph.paths_to_track(H, only_non_zero=True) == 5
+    assert ph.paths_to_track(H) == 6
+
+
 def test_mixed_cells_are_fine_and_lifting_independent():
     sup = ph.support_coefficients(hc.cyclic(5))[0]
     vols = []
@@ -140,6 +152,21 @@ def test_oracle_polyhedral_counts(torus, npaths, nsucc):
     assert len(S) == npaths
     codes, xs, _ = po.track(T, S)
     assert (codes == 1).sum() == nsucc
+
+
+def test_oracle_binomial_supports_only():
+    # y^2 + z = z^3 - y = 0 with only_non_zero: both supports are binomials, so the cell is
+    # the whole system and no toric weight is nonzero; 5 solutions in the torus
+    import polyhedral_oracle as po
+
+    y, z = hc.variables(2)
+    H = hc.System.from_polys([y ** 2 + z, z ** 3 - y])
+    T, S = ph.polyhedral(H, only_non_zero=True, seed=2)
+    assert len(S) == 5
+    codes, xs, _ = po.track(T, S)
+    assert (codes == 1).all()
+    for x in xs:
+        assert np.abs(H.evaluate(x)).max() < 1e-12
 
 
 def test_oracle_polyhedral_cyclic5():
