@@ -170,10 +170,12 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload in ("uneven", "polyhedral"):
+    if args.workload == "uneven":
         print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable": "the reference CPU arm is timed on "
-                          "the dense headline workload only"}), flush=True)
+                          "the single-system workloads only"}), flush=True)
         return
+    if args.workload == "polyhedral":
+        return run_reference_polyhedral(args)
     H, S = workload(args.seed, args.workload)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import hco
@@ -204,6 +206,49 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_reference_polyhedral(args):
+    """--impl reference --workload polyhedral: the oracle's polyhedral tracker (both stages, C++
+    restatement of the reference PolyhedralTracker) on all host threads, on an evenly spaced
+    sample of the start solutions per step."""
+    import hcgpu as hc
+    from hcgpu import polyhedral_homotopy as ph
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import hco
+    import polyhedral_oracle as po
+
+    hco.build()
+    F, _ = hc.sparse_random_system(8, 8, 4, seed=args.seed)
+    T, S = ph.polyhedral(F, seed=args.seed + 1)
+    cores = os.cpu_count()
+    sample = min(args.cpu_sample, len(S))
+    idx = np.linspace(0, len(S) - 1, sample).astype(np.int64)
+    sub = ph.PolyhedralStartSolutions(S.supports, S.start_coefficients, S.lifting, S.cells,
+                                      cell_of=S.cell_of[idx], x=S.x[idx])
+    for _ in range(args.warmup):
+        po.track(T, ph.PolyhedralStartSolutions(S.supports, S.start_coefficients, S.lifting, S.cells,
+                                                cell_of=sub.cell_of[:64], x=sub.x[:64]), nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        po.track(T, sub, nthreads=cores)
+        times.append(time.perf_counter() - t)
+    ms = 1000 * float(np.mean(times))
+    value = sample / (ms / 1000)
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded complex Gaussian coefficients)",
+        "impl": "reference",
+        "config": {"workload": WORKLOADS["polyhedral"], "seed": args.seed, "sample_paths": sample, "paths": len(S)},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} evenly spaced start solutions of {len(S)} per step, both stages; "
+                                   f"HomotopyContinuation.jl needs Julia (not installed), so the C++ restatement "
+                                   f"of its tracker runs instead"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
 
 
 def main():
