@@ -169,6 +169,16 @@ def test_oracle_binomial_supports_only():
         assert np.abs(H.evaluate(x)).max() < 1e-12
 
 
+def test_oracle_polyhedral_cyclic7():
+    # test/polyhedral_test.jl:43-46: 924 solutions of cyclic-7, on the oracle
+    import polyhedral_oracle as po
+
+    T, S = ph.polyhedral(hc.cyclic(7), seed=6)
+    assert len(S) == 924
+    codes, xs, _ = po.track(T, S)
+    assert (codes == 1).sum() == 924
+
+
 def test_oracle_polyhedral_cyclic5():
     # test/polyhedral_test.jl:38-42: 70 solutions of cyclic-5
     import polyhedral_oracle as po
