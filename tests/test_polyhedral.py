@@ -80,6 +80,14 @@ def test_univariate_and_zero_solutions():
     assert sum(r.is_success() for r in T.track_arrays(S)) == 5
 
 
+def test_polyhedral_solutions_certified():
+    # every solution the polyhedral solve of cyclic-5 returns is certified, and all 70 distinct
+    R = hc.solve(hc.cyclic(5), start_system="polyhedral", seed=2)
+    C = hc.certify(hc.cyclic(5), R)
+    assert C.ncertified() == 70
+    assert C.ndistinct_certified() == 70
+
+
 def test_solve_polyhedral_affine_sqr():
     # test/solve_test.jl:95-100: 2 solutions
     x, y = hc.variables(2)
