@@ -1803,11 +1803,13 @@ struct PathTracker {
     predict(t, Dt);
     norm_update(ld(xh));
     NewtonResult res;
-    if (MIXED && !j64 && (ss.Ds() < 1e-6 * fast_abs(t) || pred_delta > 1e-3)) {
+    if (MIXED && !j64 &&
+        (ss.Ds() < 1e-6 * fast_abs(t) || pred_delta > 1e-3 || vnorm(ld(x), nullptr) > 1e4)) {
       // With an FP32 Jacobian Newton contracts only linearly (κ ≈ cond(J)·2^-23); the
       // quadratic model behind ω = 2‖Δx₁‖/‖Δx₀‖² then reads κ as curvature, ω grows as the
-      // steps shrink and the steps shrink as ω grows. A tiny step relative to t, or a
-      // predictor solve error δ ≈ κ above 1e-3, moves the path to FP64 for good.
+      // steps shrink and the steps shrink as ω grows. A tiny step relative to t, a predictor
+      // solve error δ ≈ κ above 1e-3, or coordinates above 1e4 (FP32 loses range and accuracy
+      // on |x|^d) move the path to FP64 for good.
       switch_to_fp64(t);
       predict(t, Dt);
     }
