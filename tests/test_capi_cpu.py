@@ -93,6 +93,38 @@ def test_argument_errors_are_status_codes():
         L.hc_destroy(h)
     else:
         assert rc == 2 and b"hc_create" in L.hc_last_error(None)
+    assert L.hc_set_toric(None, 2, 1, None, None, None, 1, None) == 1
+    assert L.hc_track_toric(None, 1, None, None, None, None, None, None, None, None) == 1
+
+
+def test_mixed_cells_entry_point():
+    """hc_mixed_cells is host code: cyclic-5's cells through the C ABI, the count reported
+    with HC_ERR_TOO_LARGE when the output is too small, and bad arguments as status codes."""
+    from hcgpu import polyhedral_homotopy as ph
+
+    L = _lib.load()
+    P = _lib.ptr
+    sup = ph.support_coefficients(hc.cyclic(5))[0]
+    n = 5
+    nterms = np.array([len(S) for S in sup], dtype=np.int32)
+    pts = np.ascontiguousarray(np.concatenate(sup), dtype=np.int32)
+    rng = np.random.default_rng(1)
+    lif = np.ascontiguousarray(rng.integers(0, 2 ** 16, size=int(nterms.sum())), dtype=np.int64)
+    cnt = np.zeros(1, dtype=np.int64)
+    idx = np.zeros((4, 2 * n), dtype=np.int32)
+    rc = L.hc_mixed_cells(n, P(nterms), P(pts), P(lif), 4, P(idx), None, None, None, P(cnt))
+    assert rc in (1, 6)  # too many cells for 4 slots, or (rarely) a non-generic lifting
+    if rc == 6:
+        k = int(cnt[0])
+        assert k > 4
+        idx = np.zeros((k, 2 * n), dtype=np.int32)
+        vol = np.zeros(k, dtype=np.int64)
+        assert L.hc_mixed_cells(n, P(nterms), P(pts), P(lif), k, P(idx), None, None, P(vol), P(cnt)) == 0
+        assert int(vol.sum()) == 70
+        assert (idx[:, 0::2] != idx[:, 1::2]).all()
+    bad = np.zeros(n, dtype=np.int32)
+    assert L.hc_mixed_cells(n, P(bad), P(pts), P(lif), 4, None, None, None, None, P(cnt)) == 1
+    assert L.hc_mixed_cells(0, P(nterms), P(pts), P(lif), 4, None, None, None, None, P(cnt)) == 1
 
 
 def test_start_solutions_order():

@@ -88,6 +88,34 @@ def test_polyhedral_solutions_certified():
     assert C.ndistinct_certified() == 70
 
 
+def test_toric_entry_point_argument_checks():
+    from hcgpu import _lib
+    from hcgpu.tracking import _Handle, make_options
+
+    L = _lib.load()
+    P = _lib.ptr
+    F = f_example()
+    eq, ex, cf = F.term_arrays()
+    h = _Handle(make_options())
+    nT = len(eq)
+    W = np.zeros((1, nT))
+    Wbad = W.copy()
+    Wbad[0, 0] = -1.0
+    assert L.hc_set_toric(h.h, 2, nT, P(eq), P(ex), P(cf), 1, P(Wbad)) == 1
+    assert L.hc_set_toric(h.h, 2, nT, P(eq), P(ex), P(cf), 1, P(W)) == 0
+    x = np.ones((1, 2), dtype=np.complex128)
+    res = np.zeros(1, dtype=_lib.RESULT_DTYPE)
+    sol = np.zeros((1, 2), dtype=np.complex128)
+    t0, t1 = np.zeros(1), np.ones(1)
+    row_bad = np.array([1], dtype=np.int32)
+    row_ok = np.array([0], dtype=np.int32)
+    assert L.hc_track_toric(h.h, 1, P(x), P(row_bad), P(t0), P(t1), None, None, P(res), P(sol)) == 1
+    assert L.hc_track_toric(h.h, 1, P(x), P(row_ok), P(-t1), P(t1), None, None, P(res), P(sol)) == 1
+    # a handle holding a toric homotopy refuses the straight-line entry points
+    assert L.hc_track(h.h, 1, P(x), 1, 1.0, 0.0, 0.0, 0.0, P(res), P(sol), None, None) == 1
+    assert b"toric" in L.hc_last_error(h.h)
+
+
 def test_solve_polyhedral_affine_sqr():
     # test/solve_test.jl:95-100: 2 solutions
     x, y = hc.variables(2)
