@@ -209,21 +209,21 @@ def solve_binomial(A, b, refine: int = 3):
     Mf = M.astype(np.float64)
     logb = np.log(b)
     diag = [int(H[i][i]) for i in range(n)]
-    sols = []
-    for ks in np.ndindex(*diag):
-        y = np.zeros(n, dtype=np.complex128)
-        for i in range(n):
-            acc = logb[i] - np.dot(Hf[i, :i], y[:i]) + 2j * np.pi * ks[i]
-            y[i] = acc / Hf[i, i]
-        z = Uf @ y
-        for _ in range(refine):
-            # angles reduced first: the residual then involves numbers of size |A|·π only
-            z = z.real + 1j * (np.mod(z.imag + np.pi, 2 * np.pi) - np.pi)
-            r = Mf @ z - logb
-            r = r.real + 1j * (np.mod(r.imag + np.pi, 2 * np.pi) - np.pi)
-            z = z - np.linalg.solve(Mf, r)
-        sols.append(np.exp(z))
-    return np.array(sols).T.reshape(n, -1)
+    # every k ∈ Π [0, H_ii) at once (rows of K), in the order of np.ndindex
+    K = np.indices(diag).reshape(n, -1).T if n else np.zeros((1, 0))
+    Y = np.zeros(K.shape, dtype=np.complex128)
+    for i in range(n):
+        acc = logb[i] - Y[:, :i] @ Hf[i, :i] + 2j * np.pi * K[:, i]
+        Y[:, i] = acc / Hf[i, i]
+    Z = Y @ Uf.T
+    Minv_T = np.linalg.inv(Mf).T
+    for _ in range(refine):
+        # angles reduced first: the residual then involves numbers of size |A|·π only
+        Z = Z.real + 1j * (np.mod(Z.imag + np.pi, 2 * np.pi) - np.pi)
+        R = Z @ Mf.T - logb[None, :]
+        R = R.real + 1j * (np.mod(R.imag + np.pi, 2 * np.pi) - np.pi)
+        Z = Z - R @ Minv_T
+    return np.exp(Z).T.reshape(n, -1)
 
 
 # --------------------------------------------------------------------------------------
