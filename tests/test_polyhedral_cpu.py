@@ -120,6 +120,19 @@ def test_binomial_general_kat(unit):
     assert len({tuple(np.round(x, 7)) for x in X.T}) == 6910
 
 
+def test_binomial_univariate_and_unimodular():
+    # x^3 = b: the three cube roots; a unimodular system has exactly one solution
+    X = ph.solve_binomial(np.array([[3]]), np.array([2.0 + 1.0j]))
+    assert X.shape == (1, 3)
+    assert np.allclose(X[0] ** 3, 2.0 + 1.0j, rtol=1e-14)
+    assert len({np.round(v, 10) for v in X[0]}) == 3
+    A = np.array([[1, 1], [0, 1]])
+    b = np.array([3.0 - 1.0j, 0.5j])
+    X = ph.solve_binomial(A, b)
+    assert X.shape == (2, 1)
+    assert _binomial_err(A, b, X) < 1e-14
+
+
 def test_cell_binomial_kat():
     # test/binomial_system_test.jl:108-121: a cell of cyclic-5 with random coefficients
     sup = ph.support_coefficients(hc.cyclic(5))[0]
