@@ -507,3 +507,48 @@ def solve_polyhedral(F: System, *, only_non_zero: bool = False, seed: Optional[i
                       endgame_options=endgame_options)
     prs = T.track_arrays(S)
     return Result(prs, seed=seed, start_system="polyhedral")
+
+
+def main(argv=None):
+    """python -m hcgpu.polyhedral_homotopy [--cyclic 7 | --sparse 8] [--seed 0]: solve cyclic-n
+    or a seeded sparse system by the polyhedral homotopy and by total degree, with counts and
+    times."""
+    import argparse
+    import json
+    import time
+
+    from .systems import cyclic, sparse_random_system, total_degree_homotopy, total_degree_start_solutions
+
+    ap = argparse.ArgumentParser(description=main.__doc__.split("\n")[0])
+    ap.add_argument("--cyclic", type=int, default=0)
+    ap.add_argument("--sparse", type=int, default=0, help="n of an n×n sparse system (8 monomials of degree ≤ 4)")
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    if a.sparse:
+        F, _ = sparse_random_system(a.sparse, 8, 4, seed=a.seed)
+        name = f"{a.sparse}x{a.sparse} sparse system (seed {a.seed})"
+    else:
+        F = cyclic(a.cyclic or 7)
+        name = f"cyclic-{a.cyclic or 7}"
+    t = time.time()
+    T, S = polyhedral(F, seed=a.seed)
+    prep = time.time() - t
+    T.track_arrays(S)  # first launch (module load, program upload)
+    t = time.time()
+    rs = T.track_arrays(S)
+    tp = time.time() - t
+    Ht = total_degree_homotopy(F, np.exp(2j * np.pi * 0.123))
+    E = EndgameTracker(Ht)
+    S2 = total_degree_start_solutions(Ht.degrees)
+    E.track_arrays(S2[:64])
+    t = time.time()
+    r2 = E.track_batch(S2)
+    td = time.time() - t
+    print(json.dumps({"system": name, "mixed_volume_paths": len(S), "cells": len(T.cells), "prep_seconds": prep,
+                      "polyhedral_seconds": tp, "polyhedral_solutions": sum(r.is_success() for r in rs),
+                      "total_degree_paths": len(S2), "total_degree_seconds": td,
+                      "total_degree_solutions": sum(r.is_success() for r in r2)}))
+
+
+if __name__ == "__main__":
+    main()
