@@ -2,6 +2,7 @@
 // handle and option management, the host-side compilation of a homotopy into a monomial
 // program with a static lane schedule, and the batched track calls.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -484,6 +485,9 @@ struct hc_handle {
   unsigned long long* d_counter = nullptr;  // [queue head + HC_NSTATS counters]
   int* h_cancel = nullptr;                  // mapped host memory
   int* d_cancel = nullptr;
+  double time_limit = 0;                    // seconds per host tracking call (0 = none)
+  std::chrono::steady_clock::time_point deadline{};
+  bool timed_out = false;
   double stats[HC_NSTATS + HC_NPHASE] = {0};
   StepModel* d_model = nullptr;  // learned step proposal (hc_set_step_model)
   // batch of homotopies (hc_set_batch): programs, instance tables per precision, work units
@@ -532,6 +536,36 @@ static int fail(hc_handle* h, int code, const std::string& msg) {
   return code;
 }
 int hc_library_fail(int code, const char* msg) { return fail(nullptr, code, msg); }
+
+// Run time limit of the host entry points (hc_set_time_limit). The clock starts when a call
+// begins; waiting for the stream polls it, and at the deadline the handle's cancel flag is
+// raised, so the kernel stops exactly as for hc_cancel: paths not yet finished report
+// terminated_unknown, finished ones keep their results.
+static void start_clock(hc_handle* h) {
+  h->timed_out = false;
+  *h->h_cancel = 0;
+  if (h->time_limit > 0)
+    h->deadline = std::chrono::steady_clock::now() +
+                  std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                      std::chrono::duration<double>(h->time_limit));
+}
+static cudaError_t wait_stream(hc_handle* h) {
+  if (!(h->time_limit > 0)) return cudaStreamSynchronize(h->stream);
+  while (true) {
+    cudaError_t e = cudaStreamQuery(h->stream);
+    if (e != cudaErrorNotReady) return e;
+    if (!h->timed_out && std::chrono::steady_clock::now() >= h->deadline) {
+      h->timed_out = true;
+      __atomic_store_n(h->h_cancel, 1, __ATOMIC_SEQ_CST);
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+// status of a host call whose kernel was stopped by hc_cancel or by the time limit
+static int stopped(hc_handle* h, const char* where) {
+  if (h->timed_out) return fail(h, HC_ERR_TIMEOUT, std::string(where) + ": time limit reached");
+  return fail(h, HC_ERR_CANCELLED, std::string(where) + ": cancelled");
+}
 static int cuda_fail(hc_handle* h, cudaError_t e, const char* where) {
   return fail(h, HC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
@@ -866,7 +900,7 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   int rc = ensure_capacity(h, npaths, n);
   if (rc != HC_OK) return rc;
   size_t nv = (size_t)npaths * n;
-  *h->h_cancel = 0;
+  start_clock(h);
   CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
   rc = hc_track_device(h, npaths, (const double*)h->d_starts, endgame, t1_re, t1_im, t0_re, t0_im, h->d_res,
                        (double*)h->d_sol, h->d_val, (double*)h->d_last, nullptr);
@@ -879,11 +913,11 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   if (out_last) CK(cudaMemcpyAsync(out_last, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   unsigned long long st[HC_NSTATS + HC_NPHASE];
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  CK(wait_stream(h));
   for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   h->retracked = 0;
   h->stats_on_host = true;
-  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
+  if (*h->h_cancel) return stopped(h, "hc_track");
   if (h->opts.step_control == HC_STEP_LEARNED && endgame) {
     // re-track the paths whose endpoints coincide with plain step control, in place
     std::vector<int64_t> idx = coincident_paths(out_results, (const double2*)out_solutions, npaths, n);
@@ -915,11 +949,11 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
                              h->stream));
       }
       CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-      CK(cudaStreamSynchronize(h->stream));
+      CK(wait_stream(h));
       for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] += (double)st[i];
       h->stats[0] -= (double)idx.size();  // paths: counted once
       h->retracked = (double)idx.size();
-      if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track: cancelled");
+      if (*h->h_cancel) return stopped(h, "hc_track");
     }
   }
   return HC_OK;
@@ -1053,7 +1087,7 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
   pa.mu = mu ? dp + 3 * npaths : nullptr;
   pa.tor_w = h->d_tor_w;
   pa.tor_row = drow;
-  *h->h_cancel = 0;
+  start_clock(h);
   CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(dp, t1, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(dp + npaths, t0, npaths * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1072,11 +1106,11 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   unsigned long long st[HC_NSTATS + HC_NPHASE];
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  CK(wait_stream(h));
   for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   h->retracked = 0;
   h->stats_on_host = true;
-  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_toric: cancelled");
+  if (*h->h_cancel) return stopped(h, "hc_track_toric");
   return HC_OK;
 }
 
@@ -1370,7 +1404,7 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
   int rc = ensure_capacity_v(h, h->btotal_paths, h->btotal_vec);
   if (rc != HC_OK) return rc;
   size_t nv = (size_t)h->btotal_vec;
-  *h->h_cancel = 0;
+  start_clock(h);
   CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
   rc = hc_track_batch_device(h, (const double*)h->d_starts, endgame, h->d_res, (double*)h->d_sol, nullptr);
   if (rc != HC_OK) return rc;
@@ -1379,11 +1413,11 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   unsigned long long st[HC_NSTATS + HC_NPHASE];
   CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  CK(wait_stream(h));
   for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] = (double)st[i];
   h->retracked = 0;
   h->stats_on_host = true;
-  if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
+  if (*h->h_cancel) return stopped(h, "hc_track_batch");
   if (h->opts.step_control == HC_STEP_LEARNED && endgame) {
     // per instance: re-track the paths whose endpoints coincide with plain step control, in place
     std::vector<BatchUnit> units;
@@ -1421,11 +1455,11 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
                            cudaMemcpyDeviceToHost, h->stream));
       }
       CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-      CK(cudaStreamSynchronize(h->stream));
+      CK(wait_stream(h));
       for (int i = 0; i < HC_NSTATS + HC_NPHASE; ++i) h->stats[i] += (double)st[i];
       h->stats[0] -= (double)units.size();
       h->retracked = (double)units.size();
-      if (*h->h_cancel) return fail(h, HC_ERR_CANCELLED, "hc_track_batch: cancelled");
+      if (*h->h_cancel) return stopped(h, "hc_track_batch");
     }
   }
   return HC_OK;
@@ -1460,6 +1494,13 @@ int hc_certify(hc_handle* h, int64_t ncand, const double* cand, int real_coeffic
 int hc_cancel(hc_handle* h) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_cancel: null handle");
   __atomic_store_n(h->h_cancel, 1, __ATOMIC_SEQ_CST);
+  return HC_OK;
+}
+
+int hc_set_time_limit(hc_handle* h, double seconds) {
+  if (!h || !(seconds >= 0) || std::isinf(seconds))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_time_limit: need a handle and a finite limit >= 0");
+  h->time_limit = seconds;
   return HC_OK;
 }
 
@@ -1568,6 +1609,20 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   if (!opts) return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: null options");
   if (opts->step_control == HC_STEP_LEARNED)
     return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: learned step control needs a handle (hc_set_step_model)");
+  if (opts->step_control != HC_STEP_PLAIN && opts->step_control != HC_STEP_EXPLORE)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: unknown step control");
+  {
+    // The compiled tables are copied from a host buffer that lives only for this call; a
+    // copy recorded into a graph would read it after it is freed. Checked before any other
+    // CUDA call so that a refused call leaves the capture intact.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+    if (ce != cudaSuccess) return cuda_fail(h, ce, "hc_track_noalloc: stream query");
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(h, HC_ERR_UNSUPPORTED,
+                  "hc_track_noalloc: the stream is being captured; the tables are copied from a temporary host "
+                  "buffer, so calls cannot be recorded into a graph");
+  }
   if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: need 1 <= n <= 32");
   if (nG < 0 || nF < 0 || (nG > 0 && (!G_eq || !G_exps || !G_coef)) || (nF > 0 && (!F_eq || !F_exps || !F_coef)))
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: bad term table");
@@ -1630,7 +1685,10 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
   la.phase = nullptr;
   const size_t smem_cap = 227 * 1024;
   int wpc = opts->warps_per_cta;
-  if (wpc <= 0) wpc = std::max(1, (int)std::min<size_t>(8, (smem_cap - T.bytes) / L.bytes));
+  if (wpc <= 0) {
+    wpc = std::max(1, (int)std::min<size_t>(8, (smem_cap - T.bytes) / L.bytes));
+    wpc = balanced_warps(wpc, opts->precision);
+  }
   size_t smem = (size_t)T.bytes + (size_t)wpc * L.bytes;
   while (wpc > 1 && smem > smem_cap) {
     --wpc;

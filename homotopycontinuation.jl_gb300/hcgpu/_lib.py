@@ -11,7 +11,7 @@ from . import _build
 
 HC_OK = 0
 STATUS = {0: "HC_OK", 1: "HC_ERR_INVALID_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NO_SYSTEM",
-          4: "HC_ERR_CANCELLED", 5: "HC_ERR_UNSUPPORTED", 6: "HC_ERR_TOO_LARGE"}
+          4: "HC_ERR_CANCELLED", 5: "HC_ERR_UNSUPPORTED", 6: "HC_ERR_TOO_LARGE", 7: "HC_ERR_TIMEOUT"}
 PREC_FP64, PREC_MIXED = 0, 1
 STEP_PLAIN, STEP_LEARNED, STEP_EXPLORE = 0, 1, 2
 
@@ -82,7 +82,7 @@ RESULT_DTYPE = np.dtype(
 # exported symbols (kept in sync with include/hcgpu.h; checked by the CPU test suite)
 EXPORTS = [
     "hc_default_options", "hc_create", "hc_destroy", "hc_set_options", "hc_set_homotopy",
-    "hc_track", "hc_track_device", "hc_cancel", "hc_last_error", "hc_last_stats", "hc_fma_peak",
+    "hc_track", "hc_track_device", "hc_cancel", "hc_set_time_limit", "hc_last_error", "hc_last_stats", "hc_fma_peak",
     "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc", "hc_set_step_model",
     "hc_mlp_num_params", "hc_mlp_forward", "hc_mlp_grad", "hc_mlp_adam",
     "hc_set_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
@@ -123,6 +123,7 @@ def load(build_if_missing: bool = True):
     L.hc_track_device.argtypes = [P, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double,
                                   ct.c_double, P, P, P, P, P]
     L.hc_cancel.argtypes = [P]
+    L.hc_set_time_limit.argtypes = [P, ct.c_double]
     L.hc_last_error.argtypes = [P]
     L.hc_last_error.restype = ct.c_char_p
     L.hc_last_stats.argtypes = [P, P, ct.c_int]

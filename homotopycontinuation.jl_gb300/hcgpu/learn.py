@@ -23,8 +23,8 @@ Pipeline (``python -m hcgpu.learn all`` from the package directory, on a GPU):
   3. tune: the confidence is chosen on 5 training systems (not the held-out ones);
   4. evaluate: 50 held-out seeded systems (seeds 2000–2049), plain FP64 vs plain mixed vs
      learned mixed: steps, time, counts, endpoint agreement.
-The model (``step_model.npz``) and the evaluation (``step_model_eval.json``) are stored beside
-this file.
+The model (``step_model.npz``) is stored beside this file; the evaluation report goes to
+``--eval-out`` (default ``step_model_eval.json`` in the working directory).
 """
 from __future__ import annotations
 
@@ -48,7 +48,7 @@ NI, NH, NO = 12, 64, 2
 NPARAMS = NH * NI + NH + NH * NH + NH + NO * NH + NO
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODEL_PATH = os.path.join(HERE, "step_model.npz")
-EVAL_PATH = os.path.join(HERE, "step_model_eval.json")
+EVAL_PATH = "step_model_eval.json"
 TRAIN_SEEDS = tuple(range(1000, 1500))
 VAL_SEEDS = TRAIN_SEEDS[-50:]
 TUNE_SEEDS = TRAIN_SEEDS[:5]

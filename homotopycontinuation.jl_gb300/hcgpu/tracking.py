@@ -261,6 +261,9 @@ class _Handle:
     def cancel(self):
         self.L.hc_cancel(self.h)
 
+    def set_time_limit(self, seconds):
+        _lib.check(self.L.hc_set_time_limit(self.h, float(seconds)), self.h)
+
     def __del__(self):
         try:
             if self.h:
@@ -334,6 +337,15 @@ class EndgameTracker:
 
     def stats(self):
         return self._h.stats()
+
+    def cancel(self):
+        """Stop a track_* call running in another thread (catch_interrupt, src/solve.jl:603-709)."""
+        self._h.cancel()
+
+    def set_time_limit(self, seconds):
+        """Run time limit of each later track_* call (0 = none); past it the call raises
+        HCError(HC_ERR_TIMEOUT)."""
+        self._h.set_time_limit(seconds)
 
 
 class Tracker:

@@ -32,7 +32,8 @@ enum hc_status {
   HC_ERR_NO_SYSTEM = 3,
   HC_ERR_CANCELLED = 4,
   HC_ERR_UNSUPPORTED = 5,
-  HC_ERR_TOO_LARGE = 6
+  HC_ERR_TOO_LARGE = 6,
+  HC_ERR_TIMEOUT = 7
 };
 
 /* Arithmetic of the corrector, predictor and LU.
@@ -159,9 +160,19 @@ int hc_mixed_cells(int n, const int32_t* nterms, const int32_t* points, const in
                    int32_t* out_indices, double* out_normals, double* out_beta, int64_t* out_volumes,
                    int64_t* out_ncells);
 
-/* Request cancellation of a running hc_track on this handle (thread-safe). Paths not yet
- * finished report TrackerCode terminated_unknown and hc_track returns HC_ERR_CANCELLED. */
+/* Request cancellation of a running hc_track, hc_track_batch or hc_track_toric on this handle
+ * (thread-safe; the call's own start clears the request). The kernel stops at the next step:
+ * paths not yet finished report terminated_unknown, finished paths keep their results, and the
+ * call returns HC_ERR_CANCELLED with every output array filled. This is solve's
+ * catch_interrupt = true (src/solve.jl:603-709: an interrupt stops the loop and the paths
+ * tracked so far are returned). */
 int hc_cancel(hc_handle* h);
+
+/* Run time limit, in seconds, of each later hc_track / hc_track_batch / hc_track_toric call on
+ * this handle (0 = none, the default). When a call runs past it, it stops as after hc_cancel and
+ * returns HC_ERR_TIMEOUT. No counterpart in the reference's solve (its closest analogue is the
+ * interrupt handling above). */
+int hc_set_time_limit(hc_handle* h, double seconds);
 
 /* Last error message of this handle (or of the library when h is NULL). */
 const char* hc_last_error(hc_handle* h);
@@ -223,7 +234,10 @@ int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_r
  * of handle-owned allocations. Compiled tables above 1 MiB - 256 bytes are rejected with
  * HC_ERR_TOO_LARGE. All calls on a device share that array: calls whose kernels overlap on
  * the GPU race and must be serialised (e.g. one stream). The first call on a device looks up
- * the array's address; make it outside any stream capture. Asynchronous on `stream`
+ * the array's address; make it outside any stream capture. The compiled tables are copied
+ * from a host buffer that lives only for the call, so a call on a stream that is being
+ * captured is refused with HC_ERR_UNSUPPORTED. step_control must be HC_STEP_PLAIN or
+ * HC_STEP_EXPLORE (learned steps need a handle's network). Asynchronous on `stream`
  * (a cudaStream_t, NULL = legacy default stream). */
 int hc_track_noalloc(const hc_options* opts, int n, int nG, const int32_t* G_eq,
                      const int32_t* G_exps, const double* G_coef, int nF, const int32_t* F_eq,

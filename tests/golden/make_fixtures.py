@@ -5,7 +5,7 @@ EndgameTracker and valuation tests are read as text from the reference checkout 
 into term tables (exponent rows + complex coefficients). Run in a container that has the
 reference sources:
 
-    python tests/golden/make_fixtures.py [/path/to/HomotopyContinuation.jl]
+    python tests/golden/make_fixtures.py /path/to/HomotopyContinuation.jl
 
 The JSON is committed; the tests never read the reference checkout.
 """
@@ -99,6 +99,26 @@ def main(ref):
     g = re.search(r"γ = ([-0-9.e]+) \+ ([0-9.e]+)im", blk)
     out["mohab"] = {**to_system(eqs, ["x", "z", "y"]), "gamma": [float(g.group(1)), float(g.group(2))],
                     "expect": {"nnonsingular": int(re.search(r"nnonsingular\(res\) == (\d+)", blk).group(1))}}
+    # multiplicity KATs: "Hyperbolic - 6,6" (dehomogenised at y = 1; 12 paths with winding
+    # number 3, 2 singular results of multiplicity 6) and "Singular 1" (z = 1; one singular
+    # solution of multiplicity 3 and one nonsingular solution)
+    blk = en[en.index('@testset "Hyperbolic - 6,6"'):en.index('@testset "Singular 1"')]
+    m = re.search(r"F = \[\n(.*?)\n\s*\]\n", blk, re.S)
+    rows = [r.strip() for r in m.group(1).split("\n") if r.strip()]
+    rows = [r.replace("y", "1") for r in rows]
+    out["hyperbolic_6_6"] = {**to_system(rows, ["x", "z"]), "expect": {
+        "n_winding": int(re.search(r"winding_number == (\d+), path_results\(res\)\) == (\d+)", blk).group(2)),
+        "winding_number": int(re.search(r"winding_number == (\d+)", blk).group(1)),
+        "nresults": int(re.search(r"nresults\(res\) == (\d+)", blk).group(1)),
+        "nsingular": int(re.search(r"nsingular\(res\) == (\d+)", blk).group(1)),
+        "multiplicity": int(re.search(r"multiplicity\(r\) == (\d+)", blk).group(1))}}
+    blk = en[en.index('@testset "Singular 1"'):en.index('@testset "Wilkinson')]
+    m = re.search(r"F = \[\n(.*?)\n\s*\]\n", blk, re.S)
+    rows = split_top_level(m.group(1).replace("\n", " "))
+    rows = [re.sub(r"\bz\b", "1", r) for r in rows]
+    out["singular_1"] = {**to_system(rows, ["x", "y"]), "expect": {
+        "nsingular": int(re.search(r"nsingular\(result\) == (\d+)", blk).group(1)),
+        "nresults_nonsingular": int(re.search(r"only_nonsingular = true\) == (\d+)", blk).group(1))}}
     # cyclic-7 expected count
     out["cyclic7"] = {"expect": {"nsolutions": int(re.search(r"cyclic\(7\).*?nsolutions\(res\) == (\d+)", en, re.S).group(1))}}
     # valuation example 3 (endgame side) system and targets
@@ -152,4 +172,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <path of a HomotopyContinuation.jl checkout>")
+    main(sys.argv[1])

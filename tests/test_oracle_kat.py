@@ -197,3 +197,33 @@ def test_taylor_coefficients():
         fd = (hco.homotopy_eval(H.G.term_arrays(), H.F.term_arrays(), H.gamma, "eval", np.array([tx[0] + e]), t)
               - hco.homotopy_eval(H.G.term_arrays(), H.F.term_arrays(), H.gamma, "eval", np.array([tx[0] - e]), t)) / (2 * eps)
         np.testing.assert_allclose(J[:, j], fd, rtol=1e-6)
+
+
+def _oracle_result(name, g):
+    from hcgpu.tracking import Result, _path_results
+
+    H = hc.total_degree_homotopy(system(name), g)
+    S = hc.total_degree_start_solutions(H.degrees)
+    res, x, val, last = track(H, S)
+    return res, Result(_path_results(res, x, val, last, S, 0.1))
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_hyperbolic_6_6_multiplicity(k):
+    # test/endgame_test.jl:7-22: 12 paths of winding number 3, 2 singular results of multiplicity 6
+    e = KAT["hyperbolic_6_6"]["expect"]
+    res, R = _oracle_result("hyperbolic_6_6", np.exp(2j * np.pi * (0.1 + k / 3)))
+    assert int((res["winding_number"] == e["winding_number"]).sum()) == e["n_winding"]
+    assert R.nresults() == e["nresults"]
+    assert hc.nsingular(R) == e["nsingular"]
+    assert all(r.multiplicity == e["multiplicity"] for r in R.path_results)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_singular_1_multiplicity(k):
+    # test/endgame_test.jl:24-36: one singular solution (multiplicity 3) and one nonsingular
+    e = KAT["singular_1"]["expect"]
+    res, R = _oracle_result("singular_1", np.exp(2j * np.pi * (0.1 + k / 3)))
+    assert hc.nsingular(R) == e["nsingular"]
+    assert R.nresults(only_nonsingular=True) == e["nresults_nonsingular"]
+    assert sorted(r.multiplicity for r in R.path_results if r.is_singular()) == [3, 3, 3]
