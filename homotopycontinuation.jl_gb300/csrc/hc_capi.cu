@@ -905,6 +905,9 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
   rc = hc_track_device(h, npaths, (const double*)h->d_starts, endgame, t1_re, t1_im, t0_re, t0_im, h->d_res,
                        (double*)h->d_sol, h->d_val, (double*)h->d_last, nullptr);
   if (rc != HC_OK) return rc;
+  // copies into pageable host memory block the host until the kernel ends: poll the time
+  // limit before them
+  if (h->time_limit > 0) CK(wait_stream(h));
   CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)npaths * sizeof(hc_path_result), cudaMemcpyDeviceToHost,
                      h->stream));
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
@@ -936,6 +939,7 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
                              t0_im, h->d_res, (double*)h->d_sol, h->d_val, (double*)h->d_last, h->stream, O,
                              h->d_plist);
       if (rc != HC_OK) return rc;
+      if (h->time_limit > 0) CK(wait_stream(h));
       for (int64_t k : idx) {
         CK(cudaMemcpyAsync(out_results + k, h->d_res + k, sizeof(hc_path_result), cudaMemcpyDeviceToHost,
                            h->stream));
@@ -1101,6 +1105,7 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
   rc = track_device_impl(h, npaths, (const double*)h->d_starts, 0, 0.0, 0.0, 1.0, 0.0, h->d_res, (double*)h->d_sol,
                          nullptr, nullptr, h->stream, O, nullptr, pa);
   if (rc != HC_OK) return rc;
+  if (h->time_limit > 0) CK(wait_stream(h));  // before the blocking copies to pageable memory
   CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)npaths * sizeof(hc_path_result), cudaMemcpyDeviceToHost,
                      h->stream));
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
@@ -1408,6 +1413,7 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
   CK(cudaMemcpyAsync(h->d_starts, starts, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
   rc = hc_track_batch_device(h, (const double*)h->d_starts, endgame, h->d_res, (double*)h->d_sol, nullptr);
   if (rc != HC_OK) return rc;
+  if (h->time_limit > 0) CK(wait_stream(h));  // before the blocking copies to pageable memory
   CK(cudaMemcpyAsync(out_results, h->d_res, (size_t)h->btotal_paths * sizeof(hc_path_result),
                      cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(out_solutions, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
@@ -1447,6 +1453,7 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
                                     h->d_runits, (int)units.size());
       CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), h->stream));
       CK(launch_batch(bl, blocks, wpc, smem, h->stream));
+      if (h->time_limit > 0) CK(wait_stream(h));
       for (const BatchUnit& u : units) {
         int64_t r = h->bpath_off[u.inst] + u.lo, e = h->bvec_off[u.inst] + (int64_t)u.lo * h->bn[u.inst];
         CK(cudaMemcpyAsync(out_results + r, h->d_res + r, sizeof(hc_path_result), cudaMemcpyDeviceToHost,

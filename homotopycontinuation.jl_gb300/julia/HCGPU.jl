@@ -1,12 +1,34 @@
-# HCGPU.jl — ccall shim that lets HomotopyContinuation.jl hand its total-degree path loop to
-# libhcgpu.so (include/hcgpu.h). Drop-in point: the per-path loop of serial_solve /
-# threaded_solve (src/solve.jl:603-709) is replaced by one hc_track call per batch; the
-# returned records become PathResult values and the reference's own Result(...) does the
-# counting (src/result.jl:102-111).
+# HCGPU.jl — ccall shim that hands HomotopyContinuation.jl's path tracking to libhcgpu.so
+# (include/hcgpu.h).
+#
+# Drop-in seam: the reference's solver is `Solver{T<:AbstractPathTracker}` (src/solve.jl:41-51)
+# and its per-path loop is `solve(S::Solver, starts)` → serial_solve / threaded_solve →
+# `track(tracker, S[k]; path_number = k)` (src/solve.jl:547-709). This module defines
+#   * `GPUTracker <: AbstractPathTracker` — built from the reference's own `EndgameTracker`
+#     (same homotopy, γ, start-system scaling, TrackerOptions and EndgameOptions), with
+#     `track(::GPUTracker, x, t₁; path_number)` (src/endgame_tracker.jl:902-914);
+#   * `solve(S::Solver{GPUTracker}, starts; ...)` — ONE hc_track call for all starts, then the
+#     reference's own `Result(path_results; seed, start_system)` (src/result.jl:102-111);
+#   * `GPUPlainTracker` with `track(::GPUPlainTracker, x, t₁, t₀)` → `TrackerResult`
+#     (src/tracker.jl:1023-1026);
+#   * `solve(args...; kwargs...)` / `solver_startsolutions(args...; kwargs...)` with the
+#     reference's signatures, which build the reference's solver (so γ, the seed and the start
+#     solutions are the reference's own) and swap its tracker for a GPUTracker.
+# Methods are only added for this module's types (no type piracy). `using HCGPU` re-exports
+# every exported name of HomotopyContinuation except `solve`, so replacing
+# `using HomotopyContinuation` by `using HCGPU` leaves `solve(F; ...)`, `total_degree`,
+# `track`, `Tracker` calls and the Result API unchanged.
 module HCGPU
 
 using HomotopyContinuation
+using Random
 const HC = HomotopyContinuation
+
+for name in names(HC)
+    name in (:solve, :HomotopyContinuation) && continue
+    @eval export $name
+end
+export solve, solver_startsolutions, GPUTracker, GPUPlainTracker, gpu
 
 const libhcgpu = get(ENV, "HCGPU_LIB", joinpath(@__DIR__, "..", "_build", "libhcgpu.so"))
 
@@ -155,31 +177,254 @@ function with_handle(f, precision)
     end
 end
 
+# ---------------------------------------------------------------------------------------
+# Path trackers for the reference's Solver
+# ---------------------------------------------------------------------------------------
+
+# hc_options from the reference's TrackerOptions / TrackerParameters (src/tracker.jl:45-140)
+# and EndgameOptions (src/endgame_tracker.jl:47-72), field by field
+function hc_options(to::HC.TrackerOptions, eo::Union{Nothing,HC.EndgameOptions}; precision = 1, step_control = 0)
+    p = to.parameters
+    o = with_fields(default_options(precision = precision);
+                    max_steps = to.max_steps, extended_precision = Int(to.extended_precision),
+                    max_step_size = to.max_step_size, max_initial_step_size = to.max_initial_step_size,
+                    min_step_size = to.min_step_size, min_rel_step_size = to.min_rel_step_size,
+                    terminate_cond = to.terminate_cond, a = p.a, beta_a = p.β_a, beta_omega_p = p.β_ω_p,
+                    beta_tau = p.β_τ, strict_beta_tau = p.strict_β_τ, min_newton_iters = p.min_newton_iters,
+                    step_control = step_control)
+    eo === nothing && return o
+    with_fields(o; endgame_start = eo.endgame_start, max_endgame_steps = eo.max_endgame_steps,
+                max_endgame_extended_steps = eo.max_endgame_extended_steps, min_cond = eo.min_cond,
+                min_cond_growth = eo.min_cond_growth, min_coord_growth = eo.min_coord_growth,
+                zero_is_at_infinity = Int(eo.zero_is_at_infinity), at_infinity_check = Int(eo.at_infinity_check),
+                only_nonsingular = Int(eo.only_nonsingular), singular_min_accuracy = eo.singular_min_accuracy,
+                max_winding_number = eo.max_winding_number, val_finite_tol = eo.val_finite_tol,
+                val_at_infinity_tol = eo.val_at_infinity_tol, sing_cond = eo.sing_cond,
+                sing_accuracy = eo.sing_accuracy, scaling_threshold = eo.scaling_threshold,
+                refine_steps = eo.refine_steps)
+end
+
+# term tables of any AbstractSystem without free parameters (compiled, interpreted or with fixed
+# parameters): System(F) rebuilds its expressions (src/model_kit/abstract_system_homotopy.jl:48)
+term_tables(F::HC.AbstractSystem) = term_tables(HC.System(F))
+
+# a handle holding the straight-line homotopy γ t G + (1 - t) F of `H`
+# (src/homotopies/straight_line_homotopy.jl:10-68)
+function homotopy_handle(H, o::HCOptions)
+    H isa HC.StraightLineHomotopy ||
+        throw(ArgumentError("libhcgpu tracks straight-line homotopies; got $(typeof(H))"))
+    Geq, Gexp, Gcf, n = term_tables(H.start)
+    Feq, Fexp, Fcf, nF = term_tables(H.target)
+    n == nF && size(H.target, 1) == n || throw(ArgumentError("libhcgpu tracks square systems"))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hc_create, libhcgpu), Cint, (Ref{HCOptions}, Ref{Ptr{Cvoid}}), Ref(o), h))
+    check(ccall((:hc_set_homotopy, libhcgpu), Cint,
+                (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Int32},
+                 Ptr{Int32}, Ptr{Float64}, Float64, Float64),
+                h[], n, length(Geq), Geq, Gexp, Gcf, length(Feq), Feq, Fexp, Fcf, real(H.γ), imag(H.γ)), h[])
+    h[], n
+end
+
+"""
+    GPUTracker(eg::EndgameTracker; precision = 1, step_control = 0)
+
+An `AbstractPathTracker` (src/endgame_tracker.jl:8) running the reference's `EndgameTracker`
+algorithm for `eg`'s homotopy on the GPU, with `eg`'s γ, start system, `TrackerOptions` and
+`EndgameOptions`. `precision`: 0 = complex FP64, 1 = FP32 Jacobians/LU/Taylor with FP64
+residuals and decisions. `step_control`: 0 = the reference's rule, 1 = the learned proposal
+(load its network with `set_step_model!` first).
+"""
+mutable struct GPUTracker <: HC.AbstractPathTracker
+    handle::Ptr{Cvoid}
+    n::Int
+    endgame_start::Float64
+    function GPUTracker(eg::HC.EndgameTracker; precision = 1, step_control = 0)
+        o = hc_options(eg.tracker.options, eg.options; precision = precision, step_control = step_control)
+        h, n = homotopy_handle(eg.tracker.homotopy, o)
+        T = new(h, n, eg.options.endgame_start)
+        finalizer(T -> ccall((:hc_destroy, libhcgpu), Cvoid, (Ptr{Cvoid},), T.handle), T)
+    end
+end
+
+"""
+    GPUPlainTracker(tracker::Tracker; precision = 1)
+
+The reference's `Tracker` (src/tracker.jl:452-479) on the GPU: `track(T, x, t₁, t₀)`.
+"""
+mutable struct GPUPlainTracker
+    handle::Ptr{Cvoid}
+    n::Int
+    function GPUPlainTracker(tr::HC.Tracker; precision = 1)
+        o = hc_options(tr.options, nothing; precision = precision)
+        h, n = homotopy_handle(tr.homotopy, o)
+        T = new(h, n)
+        finalizer(T -> ccall((:hc_destroy, libhcgpu), Cvoid, (Ptr{Cvoid},), T.handle), T)
+    end
+end
+
+"`gpu(eg::EndgameTracker)` / `gpu(tracker::Tracker)`: the GPU tracker of a reference tracker."
+gpu(eg::HC.EndgameTracker; kw...) = GPUTracker(eg; kw...)
+gpu(tr::HC.Tracker; kw...) = GPUPlainTracker(tr; kw...)
+
+"""
+    set_step_model!(T::GPUTracker, params, mean, std; confidence = 0.8, max_factor = 6.0)
+
+Load the step-proposal network (hc_set_step_model): `params` the FP32 parameters
+(`hc_mlp_num_params()` values), `mean`/`std` the 12 feature normalisations.
+"""
+function set_step_model!(T::GPUTracker, params::Vector{Float32}, mean::Vector{Float32}, std::Vector{Float32};
+                         confidence = 0.8, max_factor = 6.0)
+    check(ccall((:hc_set_step_model, libhcgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Float64, Float64),
+                T.handle, params, mean, std, confidence, max_factor), T.handle)
+    T
+end
+
+# one hc_track call over all start solutions (endgame = 1: EndgameTracker, 0: Tracker)
+function track_all(h::Ptr{Cvoid}, n::Int, starts, endgame, t₁, t₀)
+    npaths = length(starts)
+    S = flat_starts(starts, n)
+    res = Vector{HCPathResult}(undef, npaths)
+    sol = Vector{Float64}(undef, 2n * npaths)
+    val = Vector{Float64}(undef, n * npaths)
+    last = Vector{Float64}(undef, 2n * npaths)
+    c1, c0 = ComplexF64(t₁), ComplexF64(t₀)
+    check(ccall((:hc_track, libhcgpu), Cint,
+                (Ptr{Cvoid}, Int64, Ptr{Float64}, Cint, Float64, Float64, Float64, Float64,
+                 Ptr{HCPathResult}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                h, npaths, S, endgame, real(c1), imag(c1), real(c0), imag(c0), res, sol, val, last), h)
+    res, sol, val, last
+end
+
+# PathResult (src/path_result.jl:76-98) of record k, as PathResult(eg) builds it
+# (src/endgame_tracker.jl:847-888)
+function path_result(r::HCPathResult, sol, val, last, k, n, start, endgame_start, path_number)
+    codes = instances(HC.EndgameTrackerCode.codes)
+    x = [complex(sol[2(n*(k-1)+i)-1], sol[2(n*(k-1)+i)]) for i in 1:n]
+    lp = [complex(last[2(n*(k-1)+i)-1], last[2(n*(k-1)+i)]) for i in 1:n]
+    HC.PathResult(return_code = Symbol(codes[r.return_code+1]), solution = x, t = r.t_re,
+                  accuracy = r.accuracy, residual = r.residual, singular = r.singular != 0,
+                  condition_jacobian = r.cond,
+                  winding_number = r.winding_number == 0 ? nothing : Int(r.winding_number),
+                  extended_precision = r.extended_precision != 0, path_number = path_number,
+                  start_solution = start, last_path_point = (lp, r.last_t),
+                  valuation = r.t_re > endgame_start ? nothing : val[n*(k-1)+1:n*k],
+                  ω = r.omega, μ = r.mu, accepted_steps = r.accepted_steps,
+                  rejected_steps = r.rejected_steps, steps_eg = r.steps_eg,
+                  extended_precision_used = r.extended_precision_used != 0)
+end
+
+function track_batch(T::GPUTracker, starts, t₁::Real = 1.0)
+    res, sol, val, last = track_all(T.handle, T.n, starts, 1, t₁, 0.0)
+    [path_result(res[k], sol, val, last, k, T.n, starts[k], T.endgame_start, k) for k in 1:length(starts)]
+end
+
+"""
+    track(T::GPUTracker, x, t₁ = 1.0; path_number = nothing) -> PathResult
+
+`track(endgame_tracker, x, t₁; path_number)` (src/endgame_tracker.jl:902-914) on the GPU (a
+batch of one path; `solve` tracks all paths in one call).
+"""
+function HC.track(T::GPUTracker, x::AbstractVector, t₁::Real = 1.0; path_number = nothing, kwargs...)
+    r = track_batch(T, [x], t₁)[1]
+    r.path_number = path_number
+    r
+end
+
+"""
+    track(T::GPUPlainTracker, x, t₁ = 1.0, t₀ = 0.0) -> TrackerResult
+
+`track(tracker, x, t₁, t₀)` (src/tracker.jl:1023-1026) on the GPU.
+"""
+function HC.track(T::GPUPlainTracker, x::AbstractVector, t₁ = 1.0, t₀ = 0.0; kwargs...)
+    res, sol, _, _ = track_all(T.handle, T.n, [x], 0, t₁, t₀)
+    r = res[1]
+    codes = instances(HC.TrackerCode.codes)
+    HC.TrackerResult(Symbol(codes[r.return_code+1]), [complex(sol[2i-1], sol[2i]) for i in 1:T.n],
+                     complex(r.t_re, r.t_im), r.accuracy, r.accepted_steps, r.rejected_steps,
+                     r.extended_precision != 0, r.extended_precision_used != 0, r.omega, r.mu, r.tau)
+end
+
+"""
+    solve(S::Solver{GPUTracker}, starts; stop_early_cb, ...) -> Result
+
+The reference's `solve(S::Solver, starts)` (src/solve.jl:547-570) with one GPU call in place
+of serial_solve / threaded_solve (src/solve.jl:603-709). With `stop_early_cb`, the results end
+after the first successful path (in path order) for which it returns true, as the reference's
+serial loop would stop there. `threading` is ignored (the GPU tracks every path at once).
+"""
+function HC.solve(S::HC.Solver{GPUTracker}, starts::AbstractArray; stop_early_cb = HC.always_false,
+                  show_progress::Bool = true, threading::Bool = true, catch_interrupt::Bool = true)
+    T = S.trackers[1]
+    st = collect(starts)
+    prs = track_batch(T, st)
+    if stop_early_cb !== HC.always_false
+        k = findfirst(r -> HC.is_success(r) && stop_early_cb(r), prs)
+        k === nothing || (prs = prs[1:k])
+    end
+    HC.Result(prs; seed = S.seed, start_system = S.start_system)
+end
+
+"""
+    solver_startsolutions(args...; precision = 1, step_control = 0, kwargs...)
+
+The reference's `solver_startsolutions` (src/solve.jl:71-214): its `Solver`, γ, seed and start
+solutions, with the tracker replaced by a `GPUTracker` when the reference built an
+`EndgameTracker` of a straight-line homotopy (total degree, or start/target systems). Other
+solvers (polyhedral, parameter or subspace homotopies) are returned unchanged.
+"""
+function solver_startsolutions(args...; precision = 1, step_control = 0, compile = false, kwargs...)
+    solver, starts = HC.solver_startsolutions(args...; compile = compile, kwargs...)
+    eg = solver.trackers[1]
+    if eg isa HC.EndgameTracker && eg.tracker.homotopy isa HC.StraightLineHomotopy
+        gt = GPUTracker(eg; precision = precision, step_control = step_control)
+        return HC.Solver(gt; seed = solver.seed, start_system = solver.start_system), starts
+    end
+    solver, starts
+end
+
+"""
+    solve(args...; precision = 1, step_control = 0, kwargs...)
+
+`solve` with the reference's arguments and keywords (src/solve.jl:447-526). Total-degree and
+start/target-system solves track on the GPU (`solver_startsolutions` above); the polyhedral
+start system (the reference's default for systems without variable groups) runs both of its
+tracking stages on the GPU (`gpu_polyhedral`); many-parameter, subspace and parameter
+homotopies go to the reference's own `solve`.
+"""
+function solve(args...; precision = 1, step_control = 0, seed = rand(UInt32), start_system = nothing,
+               target_parameters = nothing, target_subspaces = nothing, start_subspace = nothing,
+               show_progress::Bool = true, threading::Bool = true, catch_interrupt::Bool = true,
+               stop_early_cb = HC.always_false, kwargs...)
+    if target_parameters !== nothing || target_subspaces !== nothing || start_subspace !== nothing ||
+       !(length(args) == 1 && args[1] isa HC.System)
+        return HC.solve(args...; seed = seed, target_parameters = target_parameters,
+                        target_subspaces = target_subspaces, start_subspace = start_subspace,
+                        show_progress = show_progress, threading = threading, catch_interrupt = catch_interrupt,
+                        stop_early_cb = stop_early_cb,
+                        (start_system === nothing ? () : (; start_system = start_system))..., kwargs...)
+    end
+    F = args[1]
+    ss = start_system === nothing ? (isnothing(HC.variable_groups(F)) ? :polyhedral : :total_degree) : start_system
+    if ss == :polyhedral
+        Random.seed!(seed)
+        R = gpu_polyhedral(F; precision = precision)
+        return HC.Result(R.path_results; seed = seed, start_system = :polyhedral)
+    end
+    solver, starts = solver_startsolutions(F; precision = precision, step_control = step_control, seed = seed,
+                                           start_system = ss, kwargs...)
+    HC.solve(solver, collect(starts); stop_early_cb = stop_early_cb, show_progress = show_progress,
+             threading = threading, catch_interrupt = catch_interrupt)
+end
+
 """
     gpu_solve(F::System; gamma = cis(2π * rand()), precision = 1)
 
-Total-degree solve of `F` on the GPU; returns the reference's `Result`.
+Total-degree solve of `F` on the GPU with the given γ; `solve(F; start_system = :total_degree,
+gamma)` of this module.
 """
-function gpu_solve(F::HC.System; gamma = cis(2π * rand()), precision = 1)
-    T = homotopy_tables(F)
-    n, npaths = T.n, length(T.starts)
-    S = flat_starts(T.starts, n)
-    with_handle(precision) do h
-        g = ComplexF64(gamma)
-        check(ccall((:hc_set_homotopy, libhcgpu), Cint,
-                    (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Int32},
-                     Ptr{Int32}, Ptr{Float64}, Float64, Float64),
-                    h, n, length(T.Geq), T.Geq, T.Gexp, T.Gcf, length(T.Feq), T.Feq, T.Fexp, T.Fcf,
-                    real(g), imag(g)), h)
-        res = Vector{HCPathResult}(undef, npaths)
-        sol = Vector{Float64}(undef, 2n * npaths)
-        check(ccall((:hc_track, libhcgpu), Cint,
-                    (Ptr{Cvoid}, Int64, Ptr{Float64}, Cint, Float64, Float64, Float64, Float64,
-                     Ptr{HCPathResult}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
-                    h, npaths, S, 1, 1.0, 0.0, 0.0, 0.0, res, sol, C_NULL, C_NULL), h)
-        to_result(res, sol, 0, 0, n, T.starts)
-    end
-end
+gpu_solve(F::HC.System; gamma = cis(2π * rand()), precision = 1) =
+    solve(F; start_system = :total_degree, gamma = gamma, precision = precision)
 
 struct HCInstanceDesc  # hc_instance_desc
     n::Int32
@@ -272,11 +517,12 @@ end
 
 # options with some fields replaced (immutable struct: rebuilt field by field)
 function with_fields(o::HCOptions; kw...)
-    HCOptions(ntuple(i -> get(kw, fieldnames(HCOptions)[i], getfield(o, i)), fieldcount(HCOptions))...)
+    HCOptions(ntuple(i -> convert(fieldtype(HCOptions, i), get(kw, fieldnames(HCOptions)[i], getfield(o, i))),
+                     fieldcount(HCOptions))...)
 end
 
 """
-    gpu_polyhedral(F::System; only_non_zero = false)
+    gpu_polyhedral(F::System; only_non_zero = false, precision = 0)
 
 `solve(F; start_system = :polyhedral)` with both tracking stages on the GPU. The mixed cells,
 the lifting, the start coefficients and the start solutions are the reference's own
@@ -285,7 +531,7 @@ of `track(::PolyhedralTracker, …)` (src/polyhedral.jl:412-484) becomes two `hc
 calls over all paths (the second for the cells whose largest weight is ≥ 10, restarted with
 weights rescaled to a maximum of 10), and the coefficient homotopy one `hc_track`.
 """
-function gpu_polyhedral(F::HC.System; only_non_zero = false)
+function gpu_polyhedral(F::HC.System; only_non_zero = false, precision = 0)
     PT, starts = HC.polyhedral(F; only_non_zero = only_non_zero)
     H = PT.toric_tracker.homotopy
     support, lifting = PT.support, PT.lifting
@@ -348,7 +594,8 @@ function gpu_polyhedral(F::HC.System; only_non_zero = false)
         # coefficient homotopy t·F(x; start) + (1 − t)·F(x; target) with the endgame
         tcf = cfs(reduce(vcat, PT.generic_tracker.tracker.homotopy.target_coeffs))
         ok = [k for k in 1:m if res[k].return_code == 1]
-        check(ccall((:hc_set_options, libhcgpu), Cint, (Ptr{Cvoid}, Ref{HCOptions}), h[], Ref(o)), h[])
+        check(ccall((:hc_set_options, libhcgpu), Cint, (Ptr{Cvoid}, Ref{HCOptions}), h[],
+                    Ref(with_fields(o; precision = precision))), h[])
         check(ccall((:hc_set_homotopy, libhcgpu), Cint,
                     (Ptr{Cvoid}, Cint, Cint, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Cint, Ptr{Int32},
                      Ptr{Int32}, Ptr{Float64}, Float64, Float64),

@@ -1324,6 +1324,7 @@ struct Tracker {
   std::vector<C> x, xh, xb;
   SegmentStepper ss;
   double Ds_prev = 0, accuracy = 0, omega = 1, omega_prev = 1, mu = EPS, tau = INF, norm_dx0 = NaN;
+  int trace_iters = 0;  // Newton iterations of the last step (step trace only)
   bool extended_prec = false, used_extended_prec = false, refined_extended_prec = false,
        keep_extended_prec = false, use_strict_beta_tau = false;
   WeightedNorm norm;
@@ -1556,8 +1557,35 @@ static void tracker_init_t0(Tracker& T, C t0, double max_initial_step_size = INF
   T.Ds_prev = 0.0;
 }
 
+// Optional step trace of one path (test infrastructure: finding the first step where two
+// trackers' decisions part). Per step, HCO_TRACE_FIELDS doubles: t (re, im), Δs tried, trust
+// region, ω and μ before the step, accepted, Newton iterations, ‖x‖∞ after, next Δs, ω and
+// accuracy after, extended precision, tracker code, endgame steps so far.
+constexpr int HCO_TRACE_FIELDS = 15;
+static bool tracker_step_impl(Tracker& T);
+static thread_local std::vector<double>* tl_trace = nullptr;
+static thread_local const long* tl_trace_eg = nullptr;
+static int64_t g_trace_path = -1;  // 0-based path index to trace (-1: none)
+static std::vector<double> g_trace;
+
 // :851-926
 static bool tracker_step(Tracker& T) {
+  const double tr_t_re = T.ss.t().re, tr_t_im = T.ss.t().im, tr_ds = T.ss.Ds(), tr_tau = T.tau,
+               tr_omega = T.omega, tr_mu = T.mu;
+  bool ok = tracker_step_impl(T);
+  if (tl_trace) {
+    double nx = 0;
+    for (const C& v : T.x) nx = std::max(nx, cabs(v));
+    double rec[HCO_TRACE_FIELDS] = {tr_t_re, tr_t_im, tr_ds, tr_tau, tr_omega, tr_mu, (double)ok,
+                                    (double)T.trace_iters, nx, T.ss.Ds(), T.omega, T.accuracy,
+                                    (double)T.extended_prec, (double)T.code,
+                                    tl_trace_eg ? (double)*tl_trace_eg : 0.0};
+    tl_trace->insert(tl_trace->end(), rec, rec + HCO_TRACE_FIELDS);
+  }
+  return ok;
+}
+
+static bool tracker_step_impl(Tracker& T) {
   C t = T.ss.t(), Dt = T.ss.Dt(), tp = T.ss.tp();
   predict(T.pred, T.xh.data(), T.x.data(), t, Dt);
   T.norm.update(T.xh.data());
@@ -1587,6 +1615,7 @@ static bool tracker_step(Tracker& T) {
     T.last_steps_failed += 1;
   }
   T.norm_dx0 = res.norm_dx0;
+  T.trace_iters = res.iters;
   update_stepsize(T, res);
   check_terminated(T);
   return !T.last_step_failed();
@@ -2197,6 +2226,9 @@ int hco_track(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const d
       hco_path_result& R = out[k];
       std::memset(&R, 0, sizeof(R));
       R.path_number = k + 1;
+      tl_trace = k == g_trace_path ? &g_trace : nullptr;
+      tl_trace_eg = &E.steps_eg;
+      if (tl_trace) tl_trace->clear();
       if (mode == 1) {
         eg_init(E, x0.data(), t1_re);
         while (E.code == EC_tracking) eg_step(E);
@@ -2430,6 +2462,16 @@ int hco_homotopy_eval(int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
     out[2 * i + 1] = u[i].im;
   }
   return 0;
+}
+
+// Step trace of one path of the next hco_track call (path: 0-based index, -1 = off); the
+// records (HCO_TRACE_FIELDS doubles each) are read with hco_get_trace.
+void hco_set_trace(int64_t path) { g_trace_path = path; }
+int64_t hco_get_trace(double* out, int64_t max_records) {
+  int64_t nrec = (int64_t)(g_trace.size() / HCO_TRACE_FIELDS);
+  int64_t m = std::min(nrec, max_records);
+  if (out && m > 0) std::memcpy(out, g_trace.data(), (size_t)m * HCO_TRACE_FIELDS * sizeof(double));
+  return nrec;
 }
 
 }  // extern "C"

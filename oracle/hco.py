@@ -203,6 +203,27 @@ def track_toric(F_terms, weights, starts, rows, t1, t0, omega=None, mu=None, opt
     return res, xs
 
 
+TRACE_FIELDS = ["t_re", "t_im", "ds", "tau", "omega", "mu", "accepted", "iters", "norm_x", "ds_next",
+                "omega_after", "accuracy", "extended_prec", "code", "steps_eg"]
+
+
+def trace_path(G_terms, F_terms, gamma, starts, path, **kw):
+    """Track ``starts`` and return (results..., per-step trace of path index ``path``)."""
+    L = lib()
+    L.hco_set_trace.argtypes = [ct.c_int64]
+    L.hco_get_trace.argtypes = [ct.c_void_p, ct.c_int64]
+    L.hco_get_trace.restype = ct.c_int64
+    L.hco_set_trace(int(path))
+    try:
+        out = track(G_terms, F_terms, gamma, starts, **kw)
+    finally:
+        L.hco_set_trace(-1)
+    nrec = L.hco_get_trace(None, 0)
+    buf = np.zeros((max(nrec, 1), len(TRACE_FIELDS)))
+    L.hco_get_trace(_ptr(buf), nrec)
+    return out, buf[:nrec]
+
+
 def ldiv(A, b):
     A = np.asfortranarray(np.asarray(A, dtype=np.complex128))
     n = A.shape[0]

@@ -4,7 +4,12 @@ monomials of degree ≤ 4 plus a constant each), 65,536 total-degree paths, most
 On such paths the endgame's at-infinity / finite decision is ill-conditioned: for paths whose
 norm reaches 1e4..1e11, perturbations at the rounding level (a different step sequence, FP32
 Jacobians) can change the outcome between at_infinity, terminated_max_extended_steps and a
-huge "success". The learned step proposal (which only acts before the endgame zone) must not
+huge "success". The step sequences of two trackers part from the first steps: the Newton
+contraction estimate ω divides a correction near the rounding floor, so another evaluation
+order moves it by 1e-9..1e-6 relative. The reference algorithm itself decides such paths
+differently under its own FAST / CONSERVATIVE step parameters (pinned on the oracle in
+test_oracle_kat.py), which is why these tests bound the differences instead of requiring
+equal codes on diverging paths. The learned step proposal (which only acts before the endgame zone) must not
 change anything else: every path that ends at a moderate-norm solution in either run has the
 same code and endpoint in both, and no solution is found twice (path jumping)."""
 import numpy as np

@@ -227,3 +227,30 @@ def test_singular_1_multiplicity(k):
     assert hc.nsingular(R) == e["nsingular"]
     assert R.nresults(only_nonsingular=True) == e["nresults_nonsingular"]
     assert sorted(r.multiplicity for r in R.path_results if r.is_singular()) == [3, 3, 3]
+
+
+def test_at_infinity_decision_depends_on_step_parameters():
+    """On the endgame-heavy system (8 sparse quartics, seed 0) the reference's at-infinity
+    heuristic (src/endgame_tracker.jl:424-499) decides two borderline paths differently when
+    only its step parameters change (src/tracker.jl:58-62): path 61576 (a solution of norm
+    2.8e6, cond 1.7e11) is found with the default parameters but declared at infinity with
+    CONSERVATIVE_TRACKER_PARAMETERS; path 22314 is at infinity by default but a singular
+    solution with FAST_TRACKER_PARAMETERS. Counts of two trackers whose step sequences differ
+    (learned step control, or another evaluation order) can therefore differ on such paths."""
+    F, g = hc.sparse_random_system(8, 8, 4, seed=0)
+    H = hc.total_degree_homotopy(F, g)
+    S = hc.total_degree_start_solutions(H.degrees)
+    fast = dict(beta_omega_p=2.0, beta_tau=0.75, strict_beta_tau=0.4)
+    conservative = dict(beta_omega_p=4.0, beta_tau=0.25, strict_beta_tau=0.1875)
+
+    def code(p, **kw):
+        res, x, _, _ = track(H, S[p:p + 1], options=hco.default_options(**kw))
+        return hc.ENDGAME_CODES[res["return_code"][0]], bool(res["singular"][0]), float(np.abs(x[0]).max())
+
+    c, sing, nx = code(61576)
+    assert (c, sing) == ("success", False) and 1e6 < nx < 1e7
+    c, sing, nx = code(61576, **conservative)
+    assert c == "at_infinity" and 1e4 < nx < 1e5
+    assert code(22314)[0] == "at_infinity"
+    c, sing, nx = code(22314, **fast)
+    assert (c, sing) == ("success", True) and nx > 1e10
