@@ -521,6 +521,46 @@ def main_uneven(args, torch, hc, _lib, local):
     e2e_s = time.perf_counter() - t0
     retracked = int(B.stats()["paths_retracked"])
     err = max_err(out_res, out_sol)
+    # roofline: the flop model of each instance's program census, weighted by its paths (the
+    # device counters are totals over the batch; an estimate, as paths of different instances
+    # take different numbers of steps)
+    from math import comb
+
+    w = np.asarray(B.npaths, dtype=np.float64) / B.total_paths
+    f64 = f32 = 0.0
+    for wi, H in zip(w, Hs):
+        nn, dmax = H.n, int(max(H.degrees))
+        census = {"monomials": comb(nn + dmax, dmax),
+                  "value_terms": sum(len(c) for c in H.F.coefficients) + 2 * nn,
+                  "jacobian_terms": sum(int((e > 0).sum()) for e in H.F.exponents) + nn}
+        a, b = flop_model({**stats, **census}, nn, args.precision)
+        f64 += wi * a
+        f32 += wi * b
+    fp64_peak, fp32_peak = _lib.fma_peak()
+    ach = f64 / (ms / 1000) / 1e12
+    roofline = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (hc_fma_peak) on this GPU",
+                "fp32_achieved": f32 / (ms / 1000) / 1e12, "fp32_peak": fp32_peak,
+                "flops_fp64_per_launch": f64, "flops_fp32_per_launch": f32,
+                "model": "per-instance program census (dense supports: C(n+d,d) monomials), weighted by paths"}
+    # CPU baseline: the oracle on every 20th instance, all its paths
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import hco
+
+        cores = os.cpu_count()
+        pick = list(range(0, len(Hs), 20))
+        npick = 0
+        t = time.perf_counter()
+        for i in pick:
+            Si = hc.total_degree_start_solutions(Hs[i].degrees)
+            hco.track(Hs[i].G.term_arrays(), Hs[i].F.term_arrays(), Hs[i].gamma, Si, nthreads=cores)
+            npick += len(Si)
+        dt = time.perf_counter() - t
+        cpu = {"value": npick / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+               "sample": f"every 20th instance ({len(pick)} instances, {npick} paths), C++ FP64 restatement of the "
+                         f"reference EndgameTracker on {cores} threads, {dt:.1f} s"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": B.total_paths / (ms / 1000), "unit": "paths/s", "n_gpus": 1,
@@ -538,8 +578,8 @@ def main_uneven(args, torch, hc, _lib, local):
                     "d2h_bytes_per_step": int(out_res.nbytes + out_sol.nbytes)},
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
-            "roofline": None,
-            "cpu_baseline": None,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
             "plain_fp64_gpu": {"value": B.total_paths / (float(np.mean(t64)) / 1000), "unit": "paths/s",
                                "counts": counts(res64)},
             "speedup_vs_plain_fp64_gpu": float(np.mean(t64)) / ms,
@@ -599,6 +639,21 @@ def main_polyhedral(args, torch, hc, _lib, local):
     for a_, b_ in zip(rs, rs64):
         if a_.is_success() and b_.is_success() and not a_.is_singular() and not b_.is_singular():
             err = max(err, float(np.abs(a_.solution - b_.solution).max() / max(np.abs(b_.solution).max(), 1e-300)))
+    # roofline: the flop model over the three launches of the last timed step (toric stage and
+    # its restart in FP64, the coefficient homotopy in --precision), from each handle's counters
+    f64 = f32 = 0.0
+    for key, hh in T._handles.items():
+        a, b = flop_model(hh.stats(), T.n, args.precision if key == "generic" else "fp64")
+        f64 += a
+        f32 += b
+    fp64_peak, fp32_peak = _lib.fma_peak()
+    ach = f64 / (ms / 1000) / 1e12
+    roofline = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (hc_fma_peak) on this GPU",
+                "fp32_achieved": f32 / (ms / 1000) / 1e12, "fp32_peak": fp32_peak,
+                "flops_fp64_per_step": f64, "flops_fp32_per_step": f32,
+                "model": "program census x device counters of the toric, restart and coefficient launches; time "
+                         "includes the host API's copies"}
     # total degree on the same system (plain FP64)
     H = hc.total_degree_homotopy(F, g)
     S2 = hc.total_degree_start_solutions(H.degrees)
@@ -643,7 +698,7 @@ def main_polyhedral(args, torch, hc, _lib, local):
                     "h2d_bytes_per_step": int(S.x.nbytes * 2), "d2h_bytes_per_step": int(S.x.nbytes * 2)},
             "gpu_launches": 3,
             "clocks": clk.summary(),
-            "roofline": None,
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "counts": counts(rs), "codes": {c: codes.count(c) for c in set(codes)},
             "plain_fp64_gpu": {"value": npaths / float(np.mean(t64)), "unit": "paths/s", "counts": counts(rs64)},

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "hc_dev.h"
+#include "hc_slp.h"
 
 namespace hcd {
 cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaStream_t stream);
@@ -523,10 +524,30 @@ struct hc_handle {
   size_t tor_w_cap = 0;
   char* d_tor_path = nullptr;  // [4 × npaths doubles: t1, t0, ω, μ][npaths int32 rows]
   size_t tor_path_cap = 0;
+  // straight-line program of F (hc_set_slp): generated source and its kernels per precision
+  bool slp = false;
+  std::string slp_src;
+  SlpModule slp_mod[2];
+  bool slp_built[2] = {false, false};
   // step log
   double* d_log = nullptr;
   unsigned long long* d_log_count = nullptr;
   long long log_cap = 0, log_lo = 0, log_hi = 0;
+};
+
+// Makes the handle's device current for the duration of an entry point and restores the
+// caller's device afterwards, so that handles on several devices can be used from one thread.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(const hc_handle* h) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != h->device && cudaSetDevice(h->device) == cudaSuccess) prev = cur;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
 };
 
 static int fail(hc_handle* h, int code, const std::string& msg) {
@@ -643,8 +664,22 @@ int hc_create(const hc_options* opts, hc_handle** out) {
   return HC_OK;
 }
 
+int hc_create_on_device(const hc_options* opts, int device, hc_handle** out) {
+  int count = 0, cur = -1;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "hc_create_on_device");
+  if (device < 0 || device >= count) return fail(nullptr, HC_ERR_INVALID_ARG, "hc_create_on_device: no such device");
+  e = cudaGetDevice(&cur);
+  if (e == cudaSuccess) e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "hc_create_on_device");
+  int rc = hc_create(opts, out);
+  cudaSetDevice(cur);
+  return rc;
+}
+
 void hc_destroy(hc_handle* h) {
   if (!h) return;
+  DeviceGuard dg(h);
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->d_prog);
   cudaFree(h->d_starts);
@@ -686,6 +721,7 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
                     const double* G_coef, int nF, const int32_t* F_eq, const int32_t* F_exps,
                     const double* F_coef, double gamma_re, double gamma_im) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_homotopy: null handle");
+  DeviceGuard dg(h);
   if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_set_homotopy: need 1 <= n <= 32");
   if (nG < 0 || nF < 0 || (nG > 0 && (!G_eq || !G_exps || !G_coef)) || (nF > 0 && (!F_eq || !F_exps || !F_coef)))
     return fail(h, HC_ERR_INVALID_ARG, "hc_set_homotopy: bad term table");
@@ -716,6 +752,68 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   h->layout = L;
   h->has_prog = true;
   h->toric = false;
+  h->slp = false;
+  return HC_OK;
+}
+
+// the kernel of the handle's straight-line program for `precision`, compiled on first use
+static int ensure_slp(hc_handle* h, int precision) {
+  const int q = precision == HC_PREC_MIXED ? 1 : 0;
+  if (h->slp_built[q]) return HC_OK;
+  std::string err;
+  int rc = slp_build(h->slp_src, q == 1, h->slp_mod[q], err);
+  if (rc != HC_OK) return fail(h, rc, "hc_set_slp: " + err);
+  h->slp_built[q] = true;
+  return HC_OK;
+}
+
+int hc_set_slp(hc_handle* h, const hc_slp* F, const int32_t* degrees, const double* scaling, double gamma_re,
+               double gamma_im) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp: null handle");
+  DeviceGuard dg(h);
+  if (!std::isfinite(gamma_re) || !std::isfinite(gamma_im))
+    return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp: gamma must be finite");
+  SlpProgram S;
+  std::string err;
+  int rc = slp_validate(F, degrees, scaling, S, err);
+  if (rc != HC_OK) return fail(h, rc, "hc_set_slp: " + err);
+  const int n = S.n;
+  // the start system's term table (s_i x_i^{D_i} - s_i) carries n, γ and the per-path layout;
+  // F itself is evaluated by the generated code
+  std::vector<int32_t> Geq, Gexp;
+  std::vector<double> Gcf;
+  for (int i = 0; i < n; ++i) {
+    for (int q = 0; q < 2; ++q) {
+      Geq.push_back(i);
+      for (int j = 0; j < n; ++j) Gexp.push_back(q == 0 && j == i ? S.degrees[i] : 0);
+      Gcf.push_back(q == 0 ? S.scaling[i] : -S.scaling[i]);
+      Gcf.push_back(0.0);
+    }
+  }
+  rc = hc_set_homotopy(h, n, (int)Geq.size(), Geq.data(), Gexp.data(), Gcf.data(), 0, nullptr, nullptr, nullptr,
+                       gamma_re, gamma_im);
+  if (rc != HC_OK) return rc;
+  h->slp_src = slp_codegen(S);
+  h->slp_built[0] = h->slp_built[1] = false;
+  h->slp = true;
+  rc = ensure_slp(h, h->opts.precision);
+  if (rc != HC_OK) h->slp = false;
+  return rc;
+}
+
+int hc_slp_source(const hc_slp* F, const int32_t* degrees, const double* scaling, char* out, int64_t capacity,
+                  int64_t* length) {
+  SlpProgram S;
+  std::string err;
+  int rc = slp_validate(F, degrees, scaling, S, err);
+  if (rc != HC_OK) return fail(nullptr, rc, "hc_slp_source: " + err);
+  std::string src = slp_codegen(S);
+  if (length) *length = (int64_t)src.size();
+  if (out && capacity > 0) {
+    size_t m = std::min<size_t>((size_t)capacity - 1, src.size());
+    memcpy(out, src.data(), m);
+    out[m] = 0;
+  }
   return HC_OK;
 }
 
@@ -771,6 +869,7 @@ int hc_track_device(hc_handle* h, int64_t npaths, const double* d_starts, int en
                     double t1_im, double t0_re, double t0_im, hc_path_result* d_results, double* d_solutions,
                     double* d_valuation, double* d_last, void* stream) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: null handle");
+  DeviceGuard dg(h);
   if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_device: call hc_set_homotopy first");
   if (h->toric) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: the handle holds a toric homotopy (hc_track_toric)");
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_device: npaths < 0");
@@ -838,13 +937,27 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
     smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
   }
   int bps = 0;
-  CK(occupancy(O.precision, wpc, smem, &bps));
+  cudaKernel_t jit = nullptr;  // the NVRTC kernel of a straight-line program
+  if (h->slp) {
+    int rc = ensure_slp(h, O.precision);
+    if (rc != HC_OK) return rc;
+    jit = h->slp_mod[O.precision == HC_PREC_MIXED ? 1 : 0].kernel;
+    CK(cudaFuncSetAttribute((const void*)jit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)jit, 32 * wpc, smem));
+  } else {
+    CK(occupancy(O.precision, wpc, smem, &bps));
+  }
   if (bps < 1) return fail(h, HC_ERR_TOO_LARGE, "hc_track_device: kernel does not fit on an SM");
   if (O.ctas_per_sm > 0) bps = std::min(bps, O.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
   CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), s));
-  CK(launch_track(la, blocks, wpc, s));
+  if (jit) {
+    void* args[] = {(void*)&la};
+    CK(cudaLaunchKernel((const void*)jit, dim3(blocks), dim3(32 * wpc), args, smem, s));
+  } else {
+    CK(launch_track(la, blocks, wpc, s));
+  }
   h->last_blocks = blocks;
   h->last_wpc = wpc;
   h->last_stream = s;
@@ -891,6 +1004,7 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
              double t0_re, double t0_im, hc_path_result* out_results, double* out_solutions, double* out_valuation,
              double* out_last) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track: null handle");
+  DeviceGuard dg(h);
   if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_track: call hc_set_homotopy first");
   if (h->toric) return fail(h, HC_ERR_INVALID_ARG, "hc_track: the handle holds a toric homotopy (hc_track_toric)");
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track: npaths < 0");
@@ -966,6 +1080,7 @@ int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, do
 int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t path_hi) {
   if (!h || capacity < 0 || path_lo < 0 || path_hi < path_lo)
     return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_log: bad argument");
+  DeviceGuard dg(h);
   if (capacity != h->log_cap) {
     cudaFree(h->d_log);
     h->d_log = nullptr;
@@ -982,6 +1097,7 @@ int hc_set_step_log(hc_handle* h, int64_t capacity, int64_t path_lo, int64_t pat
 int hc_get_step_log(hc_handle* h, double* out, int64_t max_records, int64_t* n_records) {
   if (!h || !n_records || max_records < 0 || (max_records > 0 && !out))
     return fail(h, HC_ERR_INVALID_ARG, "hc_get_step_log: bad argument");
+  DeviceGuard dg(h);
   *n_records = 0;
   if (h->log_cap == 0) return HC_OK;
   unsigned long long cnt = 0;
@@ -1007,6 +1123,7 @@ static uint16_t to_bf16(float f) {  // round to nearest even; NaN stays NaN
 int hc_set_toric(hc_handle* h, int n, int nF, const int32_t* F_eq, const int32_t* F_exps, const double* F_coef,
                  int nrows, const double* weights) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: null handle");
+  DeviceGuard dg(h);
   if (n < 1 || n > 32) return fail(h, HC_ERR_UNSUPPORTED, "hc_set_toric: need 1 <= n <= 32");
   if (nF < 1 || !F_eq || !F_exps || !F_coef) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: bad term table");
   if (nrows < 1 || !weights) return fail(h, HC_ERR_INVALID_ARG, "hc_set_toric: need at least one weight row");
@@ -1051,6 +1168,7 @@ int hc_set_toric(hc_handle* h, int n, int nF, const int32_t* F_eq, const int32_t
   h->layout = L;
   h->has_prog = true;
   h->toric = true;
+  h->slp = false;
   h->tor_rows = nrows;
   return HC_OK;
 }
@@ -1059,6 +1177,7 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
                    const double* t0, const double* omega, const double* mu, hc_path_result* out_results,
                    double* out_solutions) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: null handle");
+  DeviceGuard dg(h);
   if (!h->has_prog || !h->toric) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_toric: call hc_set_toric first");
   if (npaths < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_track_toric: npaths < 0");
   if (npaths == 0) return HC_OK;
@@ -1122,6 +1241,7 @@ int hc_track_toric(hc_handle* h, int64_t npaths, const double* starts, const int
 int hc_set_step_model(hc_handle* h, const float* params, const float* mean, const float* std, double confidence,
                       double max_factor) {
   if (!h || !params || !mean || !std) return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: null pointer");
+  DeviceGuard dg(h);
   if (!(confidence > 0.0 && confidence < 1.0) || !(max_factor >= 1.0 && max_factor <= 1e3))
     return fail(h, HC_ERR_INVALID_ARG, "hc_set_step_model: need 0 < confidence < 1 and 1 <= max_factor <= 1000");
   const int np = hc_mlp_num_params();
@@ -1159,6 +1279,7 @@ int hc_set_step_model(hc_handle* h, const float* params, const float* mean, cons
 int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, const int32_t* unit_paths,
                  int64_t* total_paths, int64_t* total_elements) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: null handle");
+  DeviceGuard dg(h);
   if (ninstances < 1 || !inst) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: need at least one instance");
   for (int i = 0; i < ninstances; ++i) {
     const hc_instance_desc& d = inst[i];
@@ -1352,6 +1473,7 @@ static BatchLaunch batch_launch(hc_handle* h, const hc_options& O, const double*
 int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_path_result* d_results,
                           double* d_solutions, void* stream) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch_device: null handle");
+  DeviceGuard dg(h);
   if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_batch_device: call hc_set_batch first");
   if (h->btotal_paths == 0) return HC_OK;
   if (!d_starts || !d_results || !d_solutions)
@@ -1403,6 +1525,7 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
 int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_result* out_results,
                    double* out_solutions) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch: null handle");
+  DeviceGuard dg(h);
   if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_track_batch: call hc_set_batch first");
   if (h->btotal_paths == 0) return HC_OK;
   if (!starts || !out_results || !out_solutions) return fail(h, HC_ERR_INVALID_ARG, "hc_track_batch: null buffer");
@@ -1475,7 +1598,9 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
 int hc_certify(hc_handle* h, int64_t ncand, const double* cand, int real_coefficients, hc_certificate* out,
                double* out_centers, double* out_enclosures) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: null handle");
+  DeviceGuard dg(h);
   if (!h->has_prog) return fail(h, HC_ERR_NO_SYSTEM, "hc_certify: call hc_set_homotopy first");
+  if (h->slp) return fail(h, HC_ERR_UNSUPPORTED, "hc_certify: not available for a straight-line program");
   if (ncand < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: ncandidates < 0");
   if (ncand == 0) return HC_OK;
   if (!cand || !out || !out_centers || !out_enclosures) return fail(h, HC_ERR_INVALID_ARG, "hc_certify: null buffer");
@@ -1519,6 +1644,7 @@ const char* hc_last_error(hc_handle* h) {
 
 int hc_last_stats(hc_handle* h, double* out, int nout) {
   if (!h || !out || nout < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_last_stats: bad argument");
+  DeviceGuard dg(h);
   if (h->last_blocks > 0 && !h->stats_on_host) {  // counters of the last device-entry-point call
     unsigned long long st[HC_NSTATS + HC_NPHASE];
     CK(cudaMemcpyAsync(st, h->d_counter + 1, sizeof(st), cudaMemcpyDeviceToHost, h->last_stream));

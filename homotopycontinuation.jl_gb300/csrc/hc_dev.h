@@ -13,7 +13,7 @@
 //
 // Shared memory of a CTA: [per-term tables, copied once per CTA][warp 0][warp 1]...
 #pragma once
-#include <cstdint>
+#include "hc_rtc.h"
 
 #include "../../include/hcgpu.h"
 

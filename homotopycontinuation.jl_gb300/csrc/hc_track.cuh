@@ -19,7 +19,7 @@
 // predictor's Taylor coefficients are complex FP32; residuals, updates, condition numbers and
 // all decisions stay FP64.
 #pragma once
-#include <type_traits>
+#include "hc_rtc.h"
 
 // heavy routines are real calls: keeps the kernel compact (compile time and I-cache)
 #define HC_NI __noinline__
@@ -531,9 +531,113 @@ struct PathTracker {
     __syncwarp();
   }
 
+#ifdef HC_SLP
+  // ---- a system given as a straight-line program: evaluators generated for it (hc_slp.cu)
+  // G_i = s_i (x_i^{D_i} - 1) of the total-degree start system and dG_i/dx_i, lane i < n
+  __device__ __forceinline__ void slp_start(c64 xi, c64& G, c64& dG) const {
+    const int i = LANE < n ? LANE : 0;
+    const int D = hcslp::slp_degree[i];
+    const double s = hcslp::slp_scaling[i];
+    const c64 p = hcslp::spow(xi, D - 1);
+    G = s * (p * xi - C64(1.0));
+    dG = (s * (double)D) * p;
+  }
+  __device__ HC_NI void slp_H_eval(const c64* xv, c64 t, c64* out) {
+    __syncwarp();
+    c64 F;
+    hcslp::eval_v<c64>(xv, LANE, F);
+    if (LANE < n) {
+      c64 G, dG;
+      slp_start(xv[LANE], G, dG);
+      out[LANE] = (gamma() * t) * G + (C64(1.0) - t) * F;
+    }
+    __syncwarp();
+  }
+  // residual r = H(x, t) in FP64 and the Jacobian in arithmetic T: lane j writes column j
+  // (A is column-major, A[j n + i] = ∂H_i/∂x_j) from its forward-mode tangents
+  template <class T>
+  __device__ HC_NI void slp_H_eval_jac(const c64* xv, c64 t) {
+    __syncwarp();
+    const c64 ts = gamma() * t, tt = C64(1.0) - t;
+    T Fi, col[hcslp::NV];
+    hcslp::eval_vt<T>(xv, LANE, Fi, col);
+    c64 F64;
+    if constexpr (std::is_same<T, c64>::value)
+      F64 = Fi;
+    else
+      hcslp::eval_v<c64>(xv, LANE, F64);
+    T* A = (T*)Ab;
+    if (LANE < n) {
+      c64 G, dG;
+      slp_start(xv[LANE], G, dG);
+      r[LANE] = ts * G + tt * F64;
+      const T tsT = conv<T>(ts), ttT = conv<T>(tt), dGT = conv<T>(dG);
+#pragma unroll
+      for (int i = 0; i < hcslp::NV; ++i) {
+        T e = ttT * col[i];
+        if (i == LANE) e = e + tsT * dGT;
+        A[LANE * n + i] = e;
+      }
+    }
+    __syncwarp();
+  }
+  __device__ HC_NI void slp_H_eval_dd(const c64* xv, c64 t, c64* out) {
+    __syncwarp();
+    cdd F;
+    hcslp::eval_v<cdd>(xv, LANE, F);
+    if (LANE < n) {
+      const cdd s = cdd_of(C64(hcslp::slp_scaling[LANE]));
+      const cdd G = s * hcslp::spow(cdd_of(xv[LANE]), hcslp::slp_degree[LANE]) - s;
+      const cdd ts = cdd_of(gamma() * t), tt = cdd_of(C64(1.0) - t);
+      out[LANE] = round_c(ts * G + tt * F);
+    }
+    __syncwarp();
+  }
+  // taylor! (K = 1: γ G(x) - F(x); K ≥ 2: order K of H(x(s), t + s) with x(s) = Σ_{k<K} tx_k s^k)
+  __device__ HC_NI void slp_H_taylor(int K, c64 t, c64* out) {
+    __syncwarp();
+    c64 Flo, Fhi;
+    if (K == 1)
+      hcslp::series1(tx0, tx1, tx2, LANE, Flo, Fhi);
+    else if (K == 2)
+      hcslp::series2(tx0, tx1, tx2, LANE, Flo, Fhi);
+    else
+      hcslp::series3(tx0, tx1, tx2, LANE, Flo, Fhi);
+    if (LANE < n) {
+      // G_i along x_i(s): s_i (x_i(s)^D - 1), four orders by repeated truncated products
+      const c64 z = C64(0.0);
+      const c64 x0 = tx0[LANE], x1 = K > 1 ? tx1[LANE] : z, x2 = K > 2 ? tx2[LANE] : z;
+      c64 p0 = C64(1.0), p1 = z, p2 = z, p3 = z;
+      for (int d = 0; d < hcslp::slp_degree[LANE]; ++d) {
+        const c64 q3 = p0 * z + p1 * x2 + p2 * x1 + p3 * x0;
+        const c64 q2 = p0 * x2 + p1 * x1 + p2 * x0;
+        const c64 q1 = p0 * x1 + p1 * x0;
+        p0 = p0 * x0;
+        p1 = q1;
+        p2 = q2;
+        p3 = q3;
+      }
+      const double sc = hcslp::slp_scaling[LANE];
+      const c64 pw[4] = {p0 - C64(1.0), p1, p2, p3};
+      const int lo = K == 1 ? 0 : K - 1, hi = K == 1 ? 0 : K;
+      const c64 glo = sc * pw[lo], ghi = sc * pw[hi];
+      if (K == 1)
+        out[LANE] = gamma() * glo - Flo;
+      else
+        out[LANE] = gamma() * (glo + t * ghi) + ((C64(1.0) - t) * Fhi - Flo);
+    }
+    __syncwarp();
+  }
+#endif
+
   // H(x,t) (src/homotopies/straight_line_homotopy.jl:96-104) → out (vector)
   __device__ HC_NI void H_eval(const c64* xv, c64 t, c64* out) {
     HC_PHASE(PH_EVAL);
+#ifdef HC_SLP
+    slp_H_eval(xv, t, out);
+    ++c_eval;
+    return;
+#endif
     if (toric) toric_coeffs(t.re);
     eval_mono64(xv);
     c64 F, G;
@@ -550,6 +654,9 @@ struct PathTracker {
   template <class T>
   __device__ HC_NI void H_eval_jac(const c64* xv, c64 t) {
     HC_PHASE(PH_EVALJ);
+#ifdef HC_SLP
+    slp_H_eval_jac<T>(xv, t);
+#else
     if (toric) toric_coeffs(t.re);
     eval_mono64(xv);
     if constexpr (std::is_same<T, c32>::value) eval_mono32(xv);
@@ -561,6 +668,7 @@ struct PathTracker {
     else
       st(r, ts * G + tt * F);
     jac_rows<T>(ts, tt);
+#endif
     Aprec = std::is_same<T, c32>::value ? 32 : 64;
     st(xJ, ld(xv));
     tJ = t;
@@ -569,6 +677,11 @@ struct PathTracker {
   // double-double residual (:81-94), rounded to FP64 on store
   __device__ HC_NI void H_eval_dd(const c64* xv, c64 t, c64* out) {
     HC_PHASE(PH_DD);
+#ifdef HC_SLP
+    slp_H_eval_dd(xv, t, out);
+    ++c_evaldd;
+    return;
+#endif
     if (toric) toric_coeffs(t.re);
     __syncwarp();
     cdd* md = (cdd*)mono64;
@@ -678,6 +791,11 @@ struct PathTracker {
   template <class T>
   __device__ HC_NI bool H_taylor(int K, c64 t, c64* out) {
     HC_PHASE(PH_TAYLOR);
+#ifdef HC_SLP
+    slp_H_taylor(K, t, out);  // FP64 series in both precisions
+    c_taylor += K;
+    return true;
+#endif
     constexpr bool F32 = std::is_same<T, c32>::value;
     __syncwarp();
     T* S = (T*)mono64;

@@ -1,0 +1,85 @@
+// hc_track_kernel.cuh — the persistent path-tracking kernel, shared by the library's own
+// translation unit (hc_kernels.cu) and the per-system kernels compiled at run time by NVRTC
+// (hc_slp.cu). Each CTA first stages the per-term coefficient tables of the homotopy in
+// shared memory (16-byte vector copies, shared by all its warps); then each warp pulls path
+// indices from a device work queue (one atomic per path, the GPU counterpart of
+// threaded_solve's atomic counter, src/solve.jl:641-669) and tracks the path to completion
+// with a PathTracker that lives in shared memory.
+#pragma once
+#include "hc_track.cuh"
+
+namespace hcd {
+
+__device__ __forceinline__ void stage(char* dst, const void* src, int bytes) {
+  const uint4* s = (const uint4*)src;
+  uint4* d = (uint4*)dst;
+  for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) d[i] = __ldg(s + i);
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void add_stats(unsigned long long* st, const PathTracker<MIXED>* T,
+                                          unsigned long long npaths_done) {
+  atomicAdd(st + 0, npaths_done);
+  atomicAdd(st + 1, T->c_evalj);
+  atomicAdd(st + 2, T->c_eval);
+  atomicAdd(st + 3, T->c_evaldd);
+  atomicAdd(st + 4, T->c_taylor);
+  atomicAdd(st + 5, T->c_lu);
+  atomicAdd(st + 6, T->c_solve);
+  atomicAdd(st + 7, T->c_taylor64);
+  atomicAdd(st + 8, T->c_switch64);
+  atomicAdd(st + 9, T->c_learned);
+  atomicAdd(st + 10, T->c_learned_rej);
+}
+template <bool MIXED>
+__device__ __forceinline__ void add_phases(unsigned long long* ph, const PathTracker<MIXED>* T) {
+#ifdef HC_PHASE_CLOCKS
+  if (ph)
+    for (int k = 0; k < HC_NPHASE; ++k) atomicAdd(ph + k, T->ph[k]);
+#endif
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Launch la) {
+  static_assert(sizeof(PathTracker<MIXED>) <= HC_STATE_BYTES, "tracker state exceeds its shared-memory slot");
+  extern __shared__ __align__(16) char smem[];
+  const TableLayout& TL = la.T;
+  stage(smem + TL.vcoef64, la.P.vcoef64, TL.n64);
+  if (MIXED) stage(smem + TL.vcoef32, la.P.vcoef32, TL.n32);
+  stage(smem + TL.vmono, la.P.vmono, TL.nmono);
+  stage(smem + TL.jcode, la.P.jcode, TL.njcode);
+  stage(smem + TL.mdef, la.P.mdef, TL.nmdef);
+  __syncthreads();
+  const int wib = threadIdx.x >> 5;
+  char* wbase = smem + TL.bytes + (size_t)wib * la.L.bytes;
+  PathTracker<MIXED>* T = (PathTracker<MIXED>*)(wbase + la.L.state);
+  T->init(&la, wbase, smem);
+  T->reset_counters();
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  unsigned long long npaths_done = 0;
+  while (true) {
+    unsigned long long k = 0;
+    if (lane == 0) k = atomicAdd(la.counter, 1ULL);
+    k = __shfl_sync(FULL, k, 0);
+    if (k >= (unsigned long long)la.npaths) break;
+    const int64_t kk = la.path_list ? la.path_list[k] : (int64_t)k;
+    if (T->cancelled()) {
+      if (lane == 0) {
+        hc_path_result R;
+        memset(&R, 0, sizeof(R));
+        R.path_number = kk + 1;
+        R.return_code = la.mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
+        la.res[kk] = R;
+      }
+      continue;
+    }
+    T->run(kk);
+    ++npaths_done;
+  }
+  __syncwarp();
+  if (lane == 0 && la.stats) add_stats(la.stats, T, npaths_done);
+  if (lane == 0) add_phases(la.phase, T);
+}
+
+}  // namespace hcd

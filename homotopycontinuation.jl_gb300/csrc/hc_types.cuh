@@ -5,8 +5,10 @@
 // 166-266 with explicitly rounded operations (__dadd_rn/__dmul_rn) so that nvcc cannot fuse
 // the error-free transforms into FMAs.
 #pragma once
-#include <cstdint>
+#include "hc_rtc.h"
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
+#endif
 
 namespace hcd {
 

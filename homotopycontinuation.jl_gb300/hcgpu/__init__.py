@@ -15,6 +15,7 @@ from .systems import (
     uneven_instances,
     variables,
 )
+from . import slp
 from .batch import BatchTracker, autotune_unit_paths, solve_batch
 from .certification import CertificationResult, SolutionCertificate, certify
 from .io import read_parameters, read_solutions, write_parameters, write_solutions

@@ -11,7 +11,8 @@ from . import _build
 
 HC_OK = 0
 STATUS = {0: "HC_OK", 1: "HC_ERR_INVALID_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NO_SYSTEM",
-          4: "HC_ERR_CANCELLED", 5: "HC_ERR_UNSUPPORTED", 6: "HC_ERR_TOO_LARGE", 7: "HC_ERR_TIMEOUT"}
+          4: "HC_ERR_CANCELLED", 5: "HC_ERR_UNSUPPORTED", 6: "HC_ERR_TOO_LARGE", 7: "HC_ERR_TIMEOUT",
+          8: "HC_ERR_COMPILE"}
 PREC_FP64, PREC_MIXED = 0, 1
 STEP_PLAIN, STEP_LEARNED, STEP_EXPLORE = 0, 1, 2
 
@@ -81,11 +82,11 @@ RESULT_DTYPE = np.dtype(
 
 # exported symbols (kept in sync with include/hcgpu.h; checked by the CPU test suite)
 EXPORTS = [
-    "hc_default_options", "hc_create", "hc_destroy", "hc_set_options", "hc_set_homotopy",
+    "hc_default_options", "hc_create", "hc_create_on_device", "hc_destroy", "hc_set_options", "hc_set_homotopy",
     "hc_track", "hc_track_device", "hc_cancel", "hc_set_time_limit", "hc_last_error", "hc_last_stats", "hc_fma_peak",
     "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc", "hc_set_step_model",
     "hc_mlp_num_params", "hc_mlp_forward", "hc_mlp_grad", "hc_mlp_adam",
-    "hc_set_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
+    "hc_set_slp", "hc_slp_source", "hc_set_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
 ]
 STEP_LOG_FIELDS = 36
 CERT_DTYPE = np.dtype([("certified", np.int32), ("realness", np.int32), ("radius", np.float64),
@@ -114,10 +115,13 @@ def load(build_if_missing: bool = True):
     P = ct.c_void_p
     L.hc_default_options.argtypes = [ct.POINTER(Options)]
     L.hc_create.argtypes = [ct.POINTER(Options), ct.POINTER(P)]
+    L.hc_create_on_device.argtypes = [ct.POINTER(Options), ct.c_int, ct.POINTER(P)]
     L.hc_destroy.argtypes = [P]
     L.hc_destroy.restype = None
     L.hc_set_options.argtypes = [P, ct.POINTER(Options)]
     L.hc_set_homotopy.argtypes = [P, ct.c_int, ct.c_int, P, P, P, ct.c_int, P, P, P, ct.c_double, ct.c_double]
+    L.hc_set_slp.argtypes = [P, P, P, P, ct.c_double, ct.c_double]
+    L.hc_slp_source.argtypes = [P, P, P, P, ct.c_int64, P]
     L.hc_track.argtypes = [P, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_double,
                            P, P, P, P]
     L.hc_track_device.argtypes = [P, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double,

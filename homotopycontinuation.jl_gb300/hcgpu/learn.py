@@ -332,6 +332,69 @@ def compare(model, seeds, paths_per_system=4096, verbose=True, baseline=None):
     return summary, per
 
 
+def constant_model(multiplier: float, like: StepModel) -> StepModel:
+    """A network that proposes the same multiplier at every step: all weights zero, output
+    biases such that log f = log(multiplier) (o2 large makes the acceptance model sharp). It
+    runs through the learned path's code unchanged — cap at 0.75 τ, fallback to the plain
+    proposal on rejection, cooldown — so it separates what the network predicts from what
+    any constant enlargement with the same safety rules gives."""
+    params = np.zeros(NPARAMS, dtype=np.float32)
+    o2 = 100.0
+    k = o2 + 0.05
+    conf = like.confidence
+    params[-2] = np.log(multiplier) + np.log(conf / (1 - conf)) / k
+    params[-1] = o2
+    return StepModel(params=params, mean=np.zeros(NFEAT, np.float32), std=np.ones(NFEAT, np.float32),
+                     confidence=conf, max_factor=like.max_factor, meta={"constant_multiplier": multiplier})
+
+
+def _duplicates(res, sol):
+    ok = (res["return_code"] == 1) & (res["singular"] == 0)
+    X = sol[ok]
+    if X.shape[0] == 0:
+        return 0
+    key = np.round(X / np.maximum(np.abs(X).max(1, keepdims=True), 1e-300), 8)
+    _, cnt = np.unique(key.view(np.complex128).reshape(len(X), -1), axis=0, return_counts=True)
+    return int((cnt > 1).sum())
+
+
+def ablation(model, seeds=EVAL_SEEDS[:10], paths_per_system=4096, multipliers=(1.5, 2.0, 3.0), verbose=True):
+    """Held-out systems, mixed precision: the reference's step rule with its default and FAST
+    parameters (src/tracker.jl:58-62), the learned proposal, and constant multipliers with the
+    learned path's cap and fallback; codes against the FP64 plain tracker, steps, time, and
+    nonsingular endpoints found twice (path jumps within the sample). Device entry point
+    (hc_track without the host's jump check is not used: the host call applies it to learned
+    and constant runs alike)."""
+    modes = {"fp64_plain": TrackerOptions(precision="fp64"),
+             "mixed_plain": TrackerOptions(precision="mixed"),
+             "mixed_fast": TrackerOptions(precision="mixed", parameters="fast"),
+             "mixed_learned": TrackerOptions(precision="mixed", step_control="learned", step_model=model)}
+    for m in multipliers:
+        modes[f"mixed_const_{m:g}"] = TrackerOptions(precision="mixed", step_control="learned",
+                                                      step_model=constant_model(m, model))
+    runs = _run_modes(modes, seeds, paths_per_system)
+    out = {}
+    for k in modes:
+        secs = steps = paths = mism = dup = retracked = 0
+        cmis = 0
+        for s in seeds:
+            res, sol, dt, st = runs[s, k]
+            r64 = runs[s, "fp64_plain"][0]
+            secs += dt
+            steps += int(res["accepted_steps"].sum() + res["rejected_steps"].sum())
+            paths += res.shape[0]
+            mism += int((res["return_code"] != r64["return_code"]).sum())
+            cmis += int(_counts(res) != _counts(r64))
+            dup += _duplicates(res, sol)
+            retracked += int(st.get("paths_retracked", 0))
+        out[k] = dict(paths_per_second=paths / secs, steps_per_path=steps / paths, code_mismatches_vs_fp64=mism,
+                      systems_with_count_mismatch=cmis, duplicate_endpoints=dup, paths_retracked=retracked,
+                      seconds=secs)
+        if verbose:
+            print(k, {a: round(b, 3) if isinstance(b, float) else b for a, b in out[k].items()}, flush=True)
+    return dict(systems=list(seeds), paths_per_system=paths_per_system, modes=out)
+
+
 def tune(model, confidences=(0.6, 0.7, 0.8, 0.9, 0.95), seeds=TUNE_SEEDS, paths_per_system=4096, verbose=True):
     """Pick the confidence with the fastest learned run whose counts and endpoints match FP64 on
     the tuning systems (training-family seeds, disjoint from the evaluation seeds)."""
@@ -360,7 +423,7 @@ def tune(model, confidences=(0.6, 0.7, 0.8, 0.9, 0.95), seeds=TUNE_SEEDS, paths_
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["all", "evaluate"])
+    ap.add_argument("what", choices=["all", "evaluate", "ablation"])
     ap.add_argument("--train-paths", type=int, default=TRAIN_PATHS)
     ap.add_argument("--eval-paths", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=4000)
@@ -379,6 +442,11 @@ def main(argv=None):
         model.save(a.out)
         print("saved", a.out, flush=True)
     model = StepModel.load(a.out)
+    if a.what == "ablation":
+        out = ablation(model, EVAL_SEEDS[:a.eval_systems], a.eval_paths)
+        with open(a.eval_out, "w") as f:
+            json.dump(out, f, indent=1)
+        return
     summ, per = compare(model, EVAL_SEEDS[:a.eval_systems], a.eval_paths)
     with open(a.eval_out, "w") as f:
         json.dump(dict(summary=summ, per_system=per, model=dict(confidence=model.confidence,

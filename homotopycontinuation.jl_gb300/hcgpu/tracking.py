@@ -186,13 +186,25 @@ class TrackerResult:
 
 
 class _Handle:
-    def __init__(self, options: _lib.Options):
+    def __init__(self, options: _lib.Options, device: Optional[int] = None):
         self.L = _lib.load()
         self.h = ct.c_void_p()
-        _lib.check(self.L.hc_create(ct.byref(options), ct.byref(self.h)))
+        if device is None:
+            _lib.check(self.L.hc_create(ct.byref(options), ct.byref(self.h)))
+        else:
+            _lib.check(self.L.hc_create_on_device(ct.byref(options), int(device), ct.byref(self.h)))
         self.n = 0
 
-    def set_homotopy(self, H: TotalDegreeHomotopy):
+    def set_homotopy(self, H):
+        from .slp import SLPHomotopy, c_program
+
+        if isinstance(H, SLPHomotopy):  # F as a straight-line program (hc_set_slp)
+            s, deg, sc, keep = c_program(H.program)
+            self._keep = (s, deg, sc, keep)
+            _lib.check(self.L.hc_set_slp(self.h, ct.byref(s), _lib.ptr(deg), _lib.ptr(sc), H.gamma.real,
+                                         H.gamma.imag), self.h)
+            self.n = H.n
+            return
         Ge, Gx, Gc = H.G.term_arrays()
         Fe, Fx, Fc = H.F.term_arrays()
         self._keep = (Ge, Gx, Gc, Fe, Fx, Fc)
@@ -307,25 +319,35 @@ class EndgameTracker:
     """src/endgame_tracker.jl:236-254: tracks from t=1 to t=0 with the valuation and
     singular endgames. ``track_batch`` tracks many start solutions in one GPU call."""
 
-    def __init__(self, H: TotalDegreeHomotopy, tracker_options=None, endgame_options=None):
+    def __init__(self, H: TotalDegreeHomotopy, tracker_options=None, endgame_options=None, devices=None):
+        """``devices``: CUDA device indices; with more than one, every call splits its paths into
+        contiguous ranges, one per device (handles on each), tracked concurrently."""
         self.homotopy = H
         self.tracker_options = tracker_options or TrackerOptions()
         self.options = endgame_options or EndgameOptions()
-        self._h = _Handle(make_options(self.tracker_options, self.options))
-        self._h.setup_step_control(self.tracker_options)
-        self._h.set_homotopy(H)
+        o = make_options(self.tracker_options, self.options)
+        self._hs = [_Handle(o, d) for d in devices] if devices else [_Handle(o)]
+        self._h = self._hs[0]
+        for h in self._hs:
+            h.setup_step_control(self.tracker_options)
+            h.set_homotopy(H)
 
     def set_homotopy(self, H):
         """Track another homotopy with the same options (e.g. new parameters)."""
         self.homotopy = H
-        self._h.set_homotopy(H)
+        for h in self._hs:
+            h.set_homotopy(H)
 
     def track_arrays(self, starts, t1: float = 1.0):
+        if len(self._hs) > 1:
+            from .parallel import track_on_handles
+
+            return track_on_handles(self._hs, starts, endgame=True, t1=t1)
         return self._h.track(starts, endgame=True, t1=t1)
 
     def track_batch(self, starts, t1: float = 1.0, path_numbers=None):
         starts = np.asarray(starts, dtype=np.complex128).reshape(-1, self.homotopy.n)
-        res, sol, val, last = self._h.track(starts, endgame=True, t1=t1)
+        res, sol, val, last = self.track_arrays(starts, t1=t1)
         if path_numbers is not None:
             res["path_number"] = np.asarray(path_numbers)
         return _path_results(res, sol, val, last, starts, self.options.endgame_start)
@@ -336,16 +358,22 @@ class EndgameTracker:
         return r
 
     def stats(self):
+        if len(self._hs) > 1:
+            from .parallel import merge_stats
+
+            return merge_stats([h.stats() for h in self._hs])
         return self._h.stats()
 
     def cancel(self):
         """Stop a track_* call running in another thread (catch_interrupt, src/solve.jl:603-709)."""
-        self._h.cancel()
+        for h in self._hs:
+            h.cancel()
 
     def set_time_limit(self, seconds):
         """Run time limit of each later track_* call (0 = none); past it the call raises
         HCError(HC_ERR_TIMEOUT)."""
-        self._h.set_time_limit(seconds)
+        for h in self._hs:
+            h.set_time_limit(seconds)
 
 
 class Tracker:
@@ -389,13 +417,14 @@ class Tracker:
         return self.track_batch(np.asarray(x)[None, :], t1, t0)[0]
 
 
-def total_degree(F: System, gamma=None, tracker_options=None, endgame_options=None, seed=None):
+def total_degree(F: System, gamma=None, tracker_options=None, endgame_options=None, seed=None, devices=None):
     """(EndgameTracker, start solutions) for the total-degree homotopy of F
-    (src/total_degree.jl:32-117). γ defaults to cis(2π u) drawn from ``seed``."""
+    (src/total_degree.jl:32-117). γ defaults to cis(2π u) drawn from ``seed``; ``devices``
+    spreads every call's paths over several GPUs."""
     if gamma is None:
         gamma = random_gamma(np.random.default_rng(seed))
     H = total_degree_homotopy(F, gamma)
-    T = EndgameTracker(H, tracker_options, endgame_options)
+    T = EndgameTracker(H, tracker_options, endgame_options, devices=devices)
     return T, total_degree_start_solutions(H.degrees)
 
 
@@ -484,7 +513,8 @@ def nfailed(R: Result):
 
 def solve(F, starts=None, start_system: str = "total_degree", *, start_parameters=None, target_parameters=None,
           transform_result=None, transform_parameters=None, flatten: bool = False, gamma=None, seed=None,
-          tracker_options=None, endgame_options=None, precision: str = "fp64", step_control: str = "plain"):
+          tracker_options=None, endgame_options=None, precision: str = "fp64", step_control: str = "plain",
+          devices=None):
     """solve(F; start_system = :total_degree | :polyhedral) (src/solve.jl:447-526): one batched
     GPU call replaces threaded_solve's per-path loop (src/solve.jl:628-709); the polyhedral start
     system tracks its toric stage and its coefficient homotopy as one launch each.
@@ -517,6 +547,7 @@ def solve(F, starts=None, start_system: str = "total_degree", *, start_parameter
     to = tracker_options or TrackerOptions()
     to.precision = precision
     to.step_control = step_control
-    T, S = total_degree(F, gamma=gamma, tracker_options=to, endgame_options=endgame_options, seed=seed)
+    T, S = total_degree(F, gamma=gamma, tracker_options=to, endgame_options=endgame_options, seed=seed,
+                        devices=devices)
     prs = T.track_batch(S)
     return Result(prs, seed=seed, start_system=start_system)

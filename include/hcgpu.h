@@ -19,7 +19,9 @@
 #ifndef HCGPU_H
 #define HCGPU_H
 
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -33,7 +35,8 @@ enum hc_status {
   HC_ERR_CANCELLED = 4,
   HC_ERR_UNSUPPORTED = 5,
   HC_ERR_TOO_LARGE = 6,
-  HC_ERR_TIMEOUT = 7
+  HC_ERR_TIMEOUT = 7,
+  HC_ERR_COMPILE = 8
 };
 
 /* Arithmetic of the corrector, predictor and LU.
@@ -89,6 +92,11 @@ int hc_default_options(hc_options* opts);
 /* Create a tracker on the current CUDA device. Replaces EndgameTracker(H; options)
  * (src/endgame_tracker.jl:243-254). */
 int hc_create(const hc_options* opts, hc_handle** out);
+/* Same on CUDA device `device` (the caller's current device is left unchanged). Every entry
+ * point taking a handle runs on the handle's device, so one host thread may drive handles on
+ * several devices: the per-device shards of a batch (src/solve.jl:628-709 shards the paths over
+ * threads; here contiguous path ranges go to devices). */
+int hc_create_on_device(const hc_options* opts, int device, hc_handle** out);
 void hc_destroy(hc_handle* h);
 int hc_set_options(hc_handle* h, const hc_options* opts);
 
@@ -103,6 +111,58 @@ int hc_set_options(hc_handle* h, const hc_options* opts);
 int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
                     const double* G_coef, int nF, const int32_t* F_eq, const int32_t* F_exps,
                     const double* F_coef, double gamma_re, double gamma_im);
+
+/* ---- Straight-line programs -----------------------------------------------------------
+ * A target system F given as a straight-line program instead of term tables: ModelKit's
+ * InstructionSequence (src/model_kit/instruction_sequence.jl:1-27) with 0-based tape slots.
+ * Ops carry the values of ModelKit's OpType (src/model_kit/operations.jl:5-49) and its
+ * semantics (:183-248); POW_INT's second input is the integer exponent itself, not a slot.
+ * The GPU evaluator supports the algebraic ops (not ACOS .. TANH, POW). */
+enum hc_op {
+  HC_OP_STOP = 0, HC_OP_CB, HC_OP_ACOS, HC_OP_ASIN, HC_OP_COS, HC_OP_COSH, HC_OP_EXP, HC_OP_INV,
+  HC_OP_INV_NOT_ZERO, HC_OP_INVSQR, HC_OP_NEG, HC_OP_SIN, HC_OP_SINH, HC_OP_SQR, HC_OP_SQRT, HC_OP_TAN,
+  HC_OP_TANH, HC_OP_IDENTITY, HC_OP_ADD, HC_OP_DIV, HC_OP_MUL, HC_OP_SUB, HC_OP_POW_INT, HC_OP_POW,
+  HC_OP_ADD3, HC_OP_MUL3, HC_OP_MULADD, HC_OP_MULSUB, HC_OP_SUBMUL, HC_OP_ADD4, HC_OP_MUL4,
+  HC_OP_MULMULADD, HC_OP_MULMULSUB
+};
+/* Instruction (instruction_sequence.jl:1-5): output slot = op(input[0..arity-1]). */
+typedef struct hc_instruction {
+  int32_t input[4];
+  int32_t op;
+  int32_t output;
+} hc_instruction;
+/* The tape: slots [0, nconstants) hold the constants (complex, re/im interleaved), slots
+ * [variables_offset, variables_offset + n) the variables x_1..x_n, every other slot below
+ * tape_size is written by exactly one instruction, after the slots it reads (instructions in
+ * order; HC_OP_STOP ends the program). outputs[i] is the slot holding F_{i+1}. */
+typedef struct hc_slp {
+  int32_t n;
+  int32_t ninstructions;
+  const hc_instruction* instructions;
+  int32_t nconstants;
+  const double* constants;
+  int32_t variables_offset;
+  int32_t tape_size;
+  const int32_t* outputs;
+} hc_slp;
+
+/* Set the straight-line homotopy H = γ t G + (1 - t) F with F given as a straight-line
+ * program and G the total-degree start system G_i = s_i (x_i^{D_i} - 1) (degrees D, scaling
+ * s; src/total_degree.jl:62,102-106). Replaces ModelKit's compile step for this system
+ * (src/model_kit/compiled_system_homotopy.jl:178-243: the program becomes source code that is
+ * compiled, and compiled systems are cached by hash, :39-57): the program is emitted as CUDA C
+ * — values, values with forward-mode derivatives (the Jacobian column of direction j in warp
+ * lane j), double-double values and Taylor series of orders 1..3, every tape value a register
+ * — and compiled with NVRTC together with the tracking kernel for this device's architecture;
+ * the cubin is cached by a hash of its source (in memory, and on disk under $HCGPU_CACHE or
+ * ~/.cache/hcgpu). hc_track / hc_track_device then run that kernel; n ≤ 32. Fails with
+ * HC_ERR_UNSUPPORTED for ops the evaluator lacks and HC_ERR_COMPILE when NVRTC fails. */
+int hc_set_slp(hc_handle* h, const hc_slp* F, const int32_t* degrees, const double* scaling, double gamma_re,
+               double gamma_im);
+/* The CUDA C source hc_set_slp generates for a program (no GPU needed): up to capacity - 1
+ * bytes and a terminating 0 into out (may be NULL); *length receives the full length. */
+int hc_slp_source(const hc_slp* F, const int32_t* degrees, const double* scaling, char* out, int64_t capacity,
+                  int64_t* length);
 
 /* Track npaths start solutions (host arrays, npaths×n complex interleaved).
  *   endgame = 1: EndgameTracker from t = t1_re to 0 (track(eg, x), src/endgame_tracker.jl:902-914),

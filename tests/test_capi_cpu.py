@@ -168,11 +168,26 @@ def test_shard_ranges_cover_batch():
             assert max(h - l for l, h in r) - min(h - l for l, h in r) <= 1
 
 
+def _placeholder_track(starts):
+    """Stand-in for a device call (no GPU here): per-path records numbered 1.. within the
+    range, a code and an endpoint that depend only on the start solution."""
+    import numpy as np
+
+    from hcgpu import _lib
+
+    res = np.zeros(len(starts), dtype=_lib.RESULT_DTYPE)
+    res["path_number"] = np.arange(1, len(starts) + 1)
+    res["return_code"] = 1 + (np.abs(starts).sum(axis=1) * 1e3).astype(np.int64) % 3
+    res["accepted_steps"] = (np.angle(starts[:, 0]) * 100).astype(np.int64)
+    return res, starts ** 2 + 1
+
+
 def _gloo_worker(rank, world, port, out):
+    import numpy as np
     import torch
     import torch.distributed as dist
 
-    from hcgpu.parallel import shard_range
+    from hcgpu.parallel import shard_range, sharded_track
 
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -181,13 +196,20 @@ def _gloo_worker(rank, world, port, out):
     dist.all_reduce(ms, op=dist.ReduceOp.MAX)
     cnt = torch.tensor([hi - lo])
     dist.all_reduce(cnt)
-    out.put((rank, lo, hi, float(ms.item()), int(cnt.item())))
+    rng = np.random.default_rng(3)
+    starts = rng.normal(size=(1001, 4)) + 1j * rng.normal(size=(1001, 4))  # same on every rank
+    res, sol = sharded_track(_placeholder_track, starts)
+    out.put((rank, lo, hi, float(ms.item()), int(cnt.item()), res.tobytes(), sol.tobytes()))
     dist.destroy_process_group()
 
 
 def test_two_rank_sharding_gloo():
     import multiprocessing as mp
     import socket
+
+    import numpy as np
+
+    from hcgpu import _lib
 
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
@@ -198,8 +220,40 @@ def test_two_rank_sharding_gloo():
     ps = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
     for p in ps:
         p.start()
+    got = sorted(q.get(timeout=120) for _ in range(2))
     for p in ps:
-        p.join(120)
-    got = sorted(q.get(timeout=10) for _ in range(2))
+        p.join(60)
     assert got[0][1:3] == (0, 500) and got[1][1:3] == (500, 1000)
     assert all(g[3] == 11.0 and g[4] == 1000 for g in got)
+    # every rank holds the whole batch, equal to tracking it as one range
+    rng = np.random.default_rng(3)
+    starts = rng.normal(size=(1001, 4)) + 1j * rng.normal(size=(1001, 4))
+    ref_res, ref_sol = _placeholder_track(starts)
+    for g in got:
+        res = np.frombuffer(g[5], dtype=_lib.RESULT_DTYPE)
+        sol = np.frombuffer(g[6], dtype=np.complex128).reshape(-1, 4)
+        assert np.array_equal(res, ref_res) and np.array_equal(sol, ref_sol)
+
+
+def test_track_on_handles_gathers_in_path_order():
+    """The one-process form over stand-in handles (no GPU): ranges, renumbering and order."""
+    import numpy as np
+
+    from hcgpu.parallel import merge_stats, track_on_handles
+
+    class FakeHandle:
+        n = 4
+
+        def track(self, starts, endgame=True, t1=1.0, t0=0.0):
+            r, x = _placeholder_track(starts)
+            return r, x, np.abs(x), x.conj()
+
+    rng = np.random.default_rng(4)
+    starts = rng.normal(size=(37, 4)) + 1j * rng.normal(size=(37, 4))
+    for k in (1, 2, 3, 5):
+        res, sol, val, last = track_on_handles([FakeHandle() for _ in range(k)], starts)
+        ref_res, ref_sol = _placeholder_track(starts)
+        assert np.array_equal(res, ref_res) and np.array_equal(sol, ref_sol)
+        assert np.array_equal(last, ref_sol.conj())
+    st = merge_stats([{"paths": 3.0, "monomials": 7.0, "clk_run": 1.0}, {"paths": 4.0, "monomials": 7.0, "clk_run": 2.0}])
+    assert st == {"paths": 7.0, "monomials": 7.0, "clk_run": 3.0}
