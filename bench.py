@@ -37,6 +37,8 @@ WORKLOADS = {
               "in {2,3}, all total-degree paths of every instance",
     "polyhedral": "polyhedral homotopy of the 8x8 sparse system of the sparse workload: mixed-volume many paths "
                   "(toric stage, then the coefficient homotopy with the endgame)",
+    "slp": "total-degree homotopy of 8 products of three complex Gaussian affine forms in 8 variables, given as a "
+           "straight-line program (NVRTC kernel), 6,561 paths; the term-table kernel on its expansion beside it",
 }
 
 
@@ -274,6 +276,8 @@ def main():
         return main_uneven(args, torch, hc, _lib, local)
     if args.workload == "polyhedral":
         return main_polyhedral(args, torch, hc, _lib, local)
+    if args.workload == "slp":
+        return main_slp(args, torch, hc, _lib, local)
     H, S = workload(args.seed + rank, args.workload)
     if args.paths:
         S = S[: args.paths]
@@ -591,6 +595,99 @@ def main_uneven(args, torch, hc, _lib, local):
             "max_rel_endpoint_err_device_call_unchecked": err_device,
             "steps_per_path": float((res["accepted_steps"] + res["rejected_steps"]).mean()),
             "steps_per_path_plain_fp64": float((res64["accepted_steps"] + res64["rejected_steps"]).mean()),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main_slp(args, torch, hc, _lib, local):
+    """A structured system as a straight-line program (hc_set_slp: CUDA C from the program,
+    compiled by NVRTC with the tracking kernel) against the term-table kernel on the same
+    system expanded (165 monomials per equation); device-resident inputs, CUDA events."""
+    from hcgpu import slp
+
+    rank = int(os.environ.get("RANK", "0"))
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        raise SystemExit("--workload slp runs on one GPU")
+    P, Fx = slp.products_of_linear_forms(8, 3, seed=args.seed)
+    g = np.exp(2j * np.pi * 0.123)
+    P.scaling = [float(np.max(np.abs(c))) for c in Fx.coefficients]
+    Htab = hc.total_degree_homotopy(Fx, g)
+    S = hc.total_degree_start_solutions(Htab.degrees)
+    npaths, n = S.shape
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    d_starts = torch.from_numpy(np.ascontiguousarray(S).view(np.float64).reshape(-1)).to(dev)
+    d_res = torch.empty(npaths * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    d_sol = torch.empty(npaths * n * 2, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    L = _lib.load()
+
+    def call(T):
+        _lib.check(L.hc_track_device(T._h.h, npaths, ct.c_void_p(d_starts.data_ptr()), 1, 1.0, 0.0, 0.0, 0.0,
+                                     ct.c_void_p(d_res.data_ptr()), ct.c_void_p(d_sol.data_ptr()), None, None,
+                                     ct.c_void_p(stream.cuda_stream)), T._h.h)
+
+    def timed(T, steps, warmup):
+        for _ in range(warmup):
+            call(T)
+        out = []
+        for _ in range(steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            call(T)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+        return float(np.mean(out)), res, d_sol.cpu().numpy().view(np.complex128).reshape(npaths, n)
+
+    to = hc.TrackerOptions(precision=args.precision, step_control=args.step_control)
+    t = time.perf_counter()
+    Ts = hc.EndgameTracker(slp.slp_homotopy(P, g), to)
+    build_s = time.perf_counter() - t
+    with ClockSampler(local) as clk:
+        ms, rs, xs = timed(Ts, args.steps, args.warmup)
+    Tt = hc.EndgameTracker(Htab, hc.TrackerOptions(precision=args.precision, step_control=args.step_control))
+    ms_t, rt, xt = timed(Tt, args.steps, args.warmup)
+    T64 = hc.EndgameTracker(Htab, hc.TrackerOptions())
+    ms64, r64, x64 = timed(T64, 1, 1)
+    ok = (rs["return_code"] == 1) & (rs["singular"] == 0) & (r64["return_code"] == 1) & (r64["singular"] == 0)
+    err = float((np.abs(xs[ok] - x64[ok]).max(1) / np.abs(x64[ok]).max(1)).max()) if ok.any() else 0.0
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(Htab, S, min(args.cpu_sample, npaths))[0]
+        cpu["sample"] += " (the expanded system)"
+    if rank == 0:
+        def counts(r):
+            rc = r["return_code"]
+            return {"nonsingular": int(((rc == 1) & (r["singular"] == 0)).sum()),
+                    "singular": int(((rc == 1) & (r["singular"] == 1)).sum()),
+                    "at_infinity": int(np.isin(rc, [2, 3]).sum()), "failed": int((~np.isin(rc, [1, 2, 3])).sum())}
+
+        line = {
+            "metric": METRIC, "value": npaths / (ms / 1000), "unit": "paths/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": "synthetic (seeded complex Gaussian coefficients, N(0,1/2) re/im)",
+            "config": {"workload": WORKLOADS["slp"], "seed": args.seed, "paths": npaths,
+                       "program_instructions": len(P._tape.instr),
+                       "expanded_terms_per_equation": len(Fx.coefficients[0]),
+                       "nvrtc_build_seconds": build_s, "precision": args.precision, "step_control": args.step_control,
+                       "l2": "256 MiB buffer written between timed steps"},
+            "e2e": None,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "roofline": None,
+            "cpu_baseline": cpu,
+            "term_table_kernel": {"value": npaths / (ms_t / 1000), "unit": "paths/s", "counts": counts(rt)},
+            "slp_vs_term_table": ms_t / ms,
+            "counts": counts(rs), "counts_identical_to_fp64_table": counts(rs) == counts(r64),
+            "codes_differing_from_fp64_table": int((rs["return_code"] != r64["return_code"]).sum()),
+            "max_rel_endpoint_err_vs_fp64_table": err,
         }
         print(json.dumps(line), flush=True)
 
