@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=12288, help="paths of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--paths", type=int, default=0, help="track only the first N paths (profiling cases)")
+    p.add_argument("--instances", type=int, default=2000, help="uneven workload: number of instances (profiling cases)")
     p.add_argument("--autotune", action="store_true",
                    help="uneven workload: tune the paths per CTA work unit for every n first")
     p.add_argument("--workload", default="dense", choices=list(WORKLOADS),
@@ -435,7 +436,7 @@ def main_uneven(args, torch, hc, _lib, local):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
         raise SystemExit("--workload uneven runs on one GPU")
-    inst = hc.uneven_instances(2000, args.seed)
+    inst = hc.uneven_instances(args.instances, args.seed)
     Hs = [hc.total_degree_homotopy(F, g) for F, g in inst]
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)

@@ -352,10 +352,13 @@ int build_program(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, con
 
 inline int pad16(size_t b) { return (int)((b + 15) & ~(size_t)15); }
 
-TableLayout make_table_layout(const HostProg& P, int precision) {
+// vc64_global: the FP64 value coefficients stay in global memory (read through L1/L2) instead of
+// being staged per CTA
+TableLayout make_table_layout(const HostProg& P, int precision, bool vc64_global = false) {
   TableLayout T{};
   int off = 0;
-  T.n64 = pad16(P.vcoef64.size() * sizeof(double2));
+  T.vc64_global = vc64_global ? 1 : 0;
+  T.n64 = vc64_global ? 0 : pad16(P.vcoef64.size() * sizeof(double2));
   T.n32 = precision == HC_PREC_MIXED ? pad16(P.vcoef32.size() * sizeof(float2)) : 0;
   T.nmono = pad16(P.vmono.size() * sizeof(uint16_t));
   T.njcode = pad16(P.jcode.size() * sizeof(uint32_t));
@@ -374,7 +377,13 @@ TableLayout make_table_layout(const HostProg& P, int precision) {
   return T;
 }
 
-WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0) {
+// Per-warp shared layout. cold = true (mixed precision): shared memory holds what the FP32
+// phases and the FP64 residual use every step — FP64 and FP32 monomials, FP32 Taylor series,
+// FP64 value and FP32 Jacobian / Taylor partial sums — and the FP64 areas of the rare steps
+// (double-double monomials and sums, FP64 series, FP64 Jacobian sums) go to a per-warp slice of
+// global memory of L.cold bytes. This roughly halves the per-warp footprint and doubles the
+// warps per SM.
+WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0, bool cold = false) {
   WarpLayout L{};
   int n = P.n;
   int vn = (n + 1) & ~1;
@@ -384,11 +393,21 @@ WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0) {
     off += (bytes + 15) & ~(size_t)15;
     return (int)o;
   };
+  auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   L.state = take(HC_STATE_BYTES);
   size_t series = (size_t)16 * (4 * (size_t)P.top + 2 * (size_t)(P.M - P.top));
-  L.mono = take(std::max({(size_t)P.M * 32, (size_t)P.M * 24, series}));
-  size_t part = std::max({(size_t)P.val.nslots * 32, (size_t)P.jac.nslots * 16, (size_t)16});
-  L.part = take(part);
+  size_t mono_all = std::max({(size_t)P.M * 32, (size_t)P.M * 24, series});
+  size_t part_all = std::max({(size_t)P.val.nslots * 32, (size_t)P.jac.nslots * 16, (size_t)16});
+  if (cold) {
+    L.mono = take(std::max({(size_t)P.M * 24, series / 2, (size_t)16}));
+    L.part = take(std::max({(size_t)P.val.nslots * 24, (size_t)P.jac.nslots * 8, (size_t)16}));
+    L.cmono = 0;
+    L.cpart = (int)up16(mono_all);
+    L.cold = (int)(up16(mono_all) + up16(part_all));
+  } else {
+    L.mono = take(mono_all);
+    L.part = take(part_all);
+  }
   L.A = take((size_t)n * n * 16);
   L.LU = take((size_t)n * n * 16);
   L.xJ = take((size_t)vn * 16);
@@ -476,6 +495,10 @@ struct hc_handle {
   size_t d_prog_bytes = 0;
   DevProg dprog{};
   WarpLayout layout{};
+  WarpLayout layout_cold{};  // mixed precision: rare FP64 areas in d_cold
+  char* d_cold = nullptr;
+  size_t cold_cap = 0;
+  int last_warp_bytes = 0, last_table_bytes = 0;
   // buffers
   double2* d_starts = nullptr;
   hc_path_result* d_res = nullptr;
@@ -688,6 +711,7 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_val);
   cudaFree(h->d_last);
   cudaFree(h->d_counter);
+  cudaFree(h->d_cold);
   cudaFree(h->d_model);
   cudaFree(h->d_bprog);
   cudaFree(h->d_binst[0]);
@@ -747,6 +771,7 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   CK(cudaMemcpyAsync(h->d_prog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   DevProg D = bind_program(P, po, h->d_prog, gamma_re, gamma_im);
+  h->layout_cold = make_warp_layout(P, 0, true);
   h->prog = std::move(P);
   h->dprog = D;
   h->layout = L;
@@ -892,8 +917,11 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   Launch la{};
   la.P = h->dprog;
   la.O = O;
-  la.L = h->layout;
-  la.T = make_table_layout(h->prog, O.precision);
+  // mixed precision on a straight-line homotopy: FP64 value coefficients read from global
+  // memory and the rare FP64 areas in the handle's cold buffer, so twice the warps fit per SM
+  const bool cold = O.precision == HC_PREC_MIXED && !h->toric;
+  la.L = cold ? h->layout_cold : h->layout;
+  la.T = make_table_layout(h->prog, O.precision, cold);
   la.npaths = npaths;
   la.starts = (const double2*)d_starts;
   la.res = d_results;
@@ -951,6 +979,22 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   if (O.ctas_per_sm > 0) bps = std::min(bps, O.ctas_per_sm);
   int64_t want = ((int64_t)npaths + wpc - 1) / wpc;
   int blocks = (int)std::min<int64_t>((int64_t)bps * h->num_sms, want);
+  if (cold) {
+    // one slice per warp of the launch; grown only, allocated when a launch first needs more
+    size_t need = (size_t)blocks * wpc * (size_t)la.L.cold;
+    if (h->cold_cap < need) {
+      CK(cudaStreamSynchronize(s));
+      cudaFree(h->d_cold);
+      h->d_cold = nullptr;
+      h->cold_cap = 0;
+      size_t cap = (size_t)bps * h->num_sms * wpc * (size_t)la.L.cold;  // the largest launch of this shape
+      CK(cudaMalloc(&h->d_cold, std::max(cap, need)));
+      h->cold_cap = std::max(cap, need);
+    }
+    la.cold = h->d_cold;
+  }
+  h->last_warp_bytes = la.L.bytes;
+  h->last_table_bytes = la.T.bytes;
   CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), s));
   if (jit) {
     void* args[] = {(void*)&la};
@@ -1666,8 +1710,8 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   all[11] = (double)h->prog.jac_terms;
   all[12] = h->last_blocks;
   all[13] = h->last_wpc;
-  all[14] = h->layout.bytes;
-  all[15] = make_table_layout(h->prog, h->opts.precision).bytes;
+  all[14] = h->last_warp_bytes ? h->last_warp_bytes : h->layout.bytes;
+  all[15] = h->last_warp_bytes ? h->last_table_bytes : make_table_layout(h->prog, h->opts.precision).bytes;
   all[16] = h->prog.top;
   all[17] = h->stats[9];
   all[18] = h->stats[10];

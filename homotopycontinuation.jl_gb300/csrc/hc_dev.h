@@ -45,6 +45,7 @@ struct TableLayout {
   int bytes;
   int vcoef64, vcoef32, vmono, jcode, mdef;
   int n64, n32, nmono, njcode, nmdef;  // sizes in bytes (multiples of 16)
+  int vc64_global;  // 1: the FP64 value coefficients are read from global memory (L1/L2), not staged
 };
 struct WarpLayout {
   int bytes;
@@ -55,6 +56,11 @@ struct WarpLayout {
   int v32;   // FP32 staging: x (FP32 Jacobians) or tx0..tx2 (FP32 Taylor series), 4 × vn c32
   int tor;   // toric homotopy: coefficients u·t^w (c64), t^w and w (double) of the current path
   int tor_n; // value terms of the toric program (0: not a toric homotopy)
+  // Mixed precision's rarely used FP64 working set — double-double monomials and partial
+  // sums, FP64 Taylor series, FP64 Jacobian partial sums — may live in a per-warp slice of
+  // global memory (Launch::cold) instead of shared memory: `cold` bytes per warp, the monomial
+  // area at cmono and the partial sums at cpart. cold == 0: those areas alias mono and part.
+  int cold, cmono, cpart;
 };
 constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
 constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
@@ -116,6 +122,7 @@ struct Launch {
   // (program term order, tor_n per row), and the row of each path
   const double* tor_w;
   const int32_t* tor_row;
+  char* cold;  // per-warp global scratch of L.cold bytes (warp w of CTA b at (b·warps + w)·L.cold)
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

@@ -168,6 +168,11 @@ struct PathTracker {
   const int2* mdef;
   c64* mono64;
   char* part;
+  // areas of the FP64 working set that mixed precision rarely touches (double-double monomials
+  // and partial sums, FP64 Taylor series, FP64 Jacobian partial sums): a global-memory slice
+  // with the cold layout, else the same shared areas as mono64 / part
+  char* mono_c;
+  char* part_c;
   char* Ab;
   char* LUb;
   c64* xJ;
@@ -256,13 +261,21 @@ struct PathTracker {
     n = P->n;
     const WarpLayout& L = la->L;
     const TableLayout& TL = la->T;
-    vcoef64 = (const c64*)(tbase + TL.vcoef64);
+    vcoef64 = TL.vc64_global ? (const c64*)la->P.vcoef64 : (const c64*)(tbase + TL.vcoef64);
     vcoef32 = (const c32*)(tbase + TL.vcoef32);
     vmono = (const uint16_t*)(tbase + TL.vmono);
     jcode = (const uint32_t*)(tbase + TL.jcode);
     mdef = (const int2*)(tbase + TL.mdef);
     mono64 = (c64*)(base + L.mono);
     part = base + L.part;
+    if (L.cold > 0 && la->cold) {
+      char* cb = la->cold + (size_t)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * (size_t)L.cold;
+      mono_c = cb + L.cmono;
+      part_c = cb + L.cpart;
+    } else {
+      mono_c = (char*)mono64;
+      part_c = part;
+    }
     Ab = base + L.A;
     LUb = base + L.LU;
     xJ = (c64*)(base + L.xJ);
@@ -482,7 +495,7 @@ struct PathTracker {
   __device__ HC_NI void jac_rows(c64 ts64, c64 tt64) {
     HC_PHASE(PH_JACROWS);
     const DevRows& R = P->jac;
-    T* pp = (T*)part;
+    T* pp = std::is_same<T, c32>::value ? (T*)part : (T*)part_c;
     const T* mv;
     const T* cf;
     if constexpr (std::is_same<T, c64>::value) {
@@ -684,7 +697,7 @@ struct PathTracker {
 #endif
     if (toric) toric_coeffs(t.re);
     __syncwarp();
-    cdd* md = (cdd*)mono64;
+    cdd* md = (cdd*)mono_c;
     if (LANE == 0) md[0] = cdd_of(C64(1.0));
     for (int L = 1; L < P->nlev; ++L) {
       int b = __ldg(P->lev + L), e = __ldg(P->lev + L + 1);
@@ -695,7 +708,7 @@ struct PathTracker {
       __syncwarp();
     }
     const DevRows& R = P->val;
-    cdd* pp = (cdd*)part;
+    cdd* pp = (cdd*)part_c;
     int s0 = __ldg(R.lane_seg + LANE), s1e = __ldg(R.lane_seg + LANE + 1);
     for (int s = s0; s < s1e; ++s) {
       int4 g = __ldg(R.seg + s);
@@ -798,7 +811,7 @@ struct PathTracker {
 #endif
     constexpr bool F32 = std::is_same<T, c32>::value;
     __syncwarp();
-    T* S = (T*)mono64;
+    T* S = F32 ? (T*)mono64 : (T*)mono_c;
     const int top = P->top;
     T* ST = S + 4 * top;
     const int lo = (K == 1) ? 0 : K - 1, hi = (K == 1) ? 0 : K;
@@ -863,7 +876,7 @@ struct PathTracker {
       }
     }
     const DevRows& R = P->val;
-    T* pp = (T*)part;
+    T* pp = F32 ? (T*)part : (T*)part_c;
     const T* cf;
     if constexpr (std::is_same<T, c64>::value)
       cf = vcoef64;
