@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <limits>
@@ -172,9 +173,11 @@ struct Term {
   C coef;
   std::vector<std::pair<int, int>> vars;  // (variable, exponent>0)
 };
+struct Slp;
 struct System {
   int n = 0, m = 0, maxdeg = 0;
   std::vector<Term> terms;
+  const Slp* slp = nullptr;  // F given as a straight-line program instead of terms
 };
 
 static System make_system(int n, int m, int nterms, const int32_t* eq, const int32_t* exps,
@@ -196,6 +199,283 @@ static System make_system(int n, int m, int nterms, const int32_t* eq, const int
     }
   }
   return S;
+}
+
+// ---------------------------------------------------------------------------------------
+// Straight-line programs: ModelKit's InstructionSequence interpreted (op semantics of
+// src/model_kit/operations.jl:183-248; Taylor rules of src/model_kit/taylor.jl). Tape slots:
+// constants [0, nconst), variables [voff, voff + n), instruction outputs above.
+// ---------------------------------------------------------------------------------------
+enum SlpOp {
+  SOP_STOP = 0, SOP_CB, SOP_ACOS, SOP_ASIN, SOP_COS, SOP_COSH, SOP_EXP, SOP_INV, SOP_INV_NOT_ZERO, SOP_INVSQR,
+  SOP_NEG, SOP_SIN, SOP_SINH, SOP_SQR, SOP_SQRT, SOP_TAN, SOP_TANH, SOP_IDENTITY, SOP_ADD, SOP_DIV, SOP_MUL,
+  SOP_SUB, SOP_POW_INT, SOP_POW, SOP_ADD3, SOP_MUL3, SOP_MULADD, SOP_MULSUB, SOP_SUBMUL, SOP_ADD4, SOP_MUL4,
+  SOP_MULMULADD, SOP_MULMULSUB
+};
+struct Slp {
+  int n = 0, voff = 0, tape = 0, nconst = 0;
+  std::vector<int> ins;  // 6 per instruction: input[0..3], op, output
+  std::vector<C> consts;
+  std::vector<int> outputs;
+};
+
+static inline DD dd_div(DD a, DD b) {  // long division: three quotient digits
+  double q1 = a.hi / b.hi;
+  DD r = a - b * dd(q1);
+  double q2 = r.hi / b.hi;
+  r = r - b * dd(q2);
+  double q3 = r.hi / b.hi;
+  double s1, e1;
+  quick_two_sum(q1, q2, s1, e1);
+  return DD{s1, e1} + dd(q3);
+}
+static inline C s_neg(C a) { return -a; }
+static inline CDD s_neg(CDD a) { return CDD{DD{-a.re.hi, -a.re.lo}, DD{-a.im.hi, -a.im.lo}}; }
+static inline C s_div(C a, C b) { return div_fast(a, b); }  // op_div = div_fast
+static inline CDD s_div(CDD a, CDD b) {
+  DD d = b.re * b.re + b.im * b.im;
+  return CDD{dd_div(a.re * b.re + a.im * b.im, d), dd_div(a.im * b.re - a.re * b.im, d)};
+}
+static inline C s_sqrt(C a) {
+  std::complex<double> r = std::sqrt(std::complex<double>(a.re, a.im));
+  return C{r.real(), r.imag()};
+}
+static inline CDD s_sqrt(CDD a) {  // FP64 root, then one Newton step in double-double
+  C s = s_sqrt(round_c(a));
+  if (s.re == 0.0 && s.im == 0.0) return cdd(s);
+  CDD sd = cdd(s);
+  C r = round_c(a - sd * sd);
+  return sd + cdd(div_fast(r, C{2.0 * s.re, 2.0 * s.im}));
+}
+static inline bool s_zero(C a) { return a.re == 0.0 && a.im == 0.0; }
+static inline bool s_zero(CDD a) { return a.re.hi == 0.0 && a.im.hi == 0.0; }
+template <class S>
+static S s_inv(S a) {
+  return s_div(one_like(a), a);
+}
+template <class S>
+static S s_pow(S a, int p) {  // power_by_squaring, inverted for p < 0 (op_pow_int)
+  unsigned q = p < 0 ? (unsigned)(-p) : (unsigned)p;
+  S r = one_like(a), b = a;
+  bool first = true;
+  while (q) {
+    if (q & 1u) {
+      r = first ? b : r * b;
+      first = false;
+    }
+    q >>= 1;
+    if (q) b = b * b;
+  }
+  return p < 0 ? s_inv(r) : r;
+}
+static inline C s_scale(C a, int k) { return a * (double)k; }
+template <class S>
+static S slp_value(int op, const S* v, int p) {
+  switch (op) {
+    case SOP_CB: return v[0] * v[0] * v[0];
+    case SOP_INV: return s_inv(v[0]);
+    case SOP_INV_NOT_ZERO: return s_zero(v[0]) ? v[0] : s_inv(v[0]);
+    case SOP_INVSQR: { S i = s_inv(v[0]); return i * i; }
+    case SOP_NEG: return s_neg(v[0]);
+    case SOP_SQR: return v[0] * v[0];
+    case SOP_SQRT: return s_sqrt(v[0]);
+    case SOP_IDENTITY: return v[0];
+    case SOP_ADD: return v[0] + v[1];
+    case SOP_DIV: return s_div(v[0], v[1]);
+    case SOP_MUL: return v[0] * v[1];
+    case SOP_SUB: return v[0] - v[1];
+    case SOP_POW_INT: return s_pow(v[0], p);
+    case SOP_ADD3: return v[0] + v[1] + v[2];
+    case SOP_MUL3: return v[0] * v[1] * v[2];
+    case SOP_MULADD: return v[0] * v[1] + v[2];
+    case SOP_MULSUB: return v[0] * v[1] - v[2];
+    case SOP_SUBMUL: return v[2] - v[0] * v[1];
+    case SOP_ADD4: return v[0] + v[1] + v[2] + v[3];
+    case SOP_MUL4: return v[0] * v[1] * v[2] * v[3];
+    case SOP_MULMULADD: return v[0] * v[1] + v[2] * v[3];
+    case SOP_MULMULSUB: return v[0] * v[1] - v[2] * v[3];
+  }
+  return zero_like(v[0]);
+}
+static int slp_arity(int op) {
+  if (op >= SOP_CB && op <= SOP_IDENTITY) return 1;
+  if (op >= SOP_ADD && op <= SOP_POW) return 2;
+  if (op >= SOP_ADD3 && op <= SOP_SUBMUL) return 3;
+  if (op >= SOP_ADD4) return 4;
+  return 0;
+}
+// all tape values at x (arithmetic S)
+template <class S>
+static void slp_tape(const Slp& P, const S* x, std::vector<S>& t) {
+  t.assign(P.tape, zero_like(x[0]));
+  for (int k = 0; k < P.nconst; ++k) t[k] = promote(P.consts[k], x[0]);
+  for (int j = 0; j < P.n; ++j) t[P.voff + j] = x[j];
+  for (size_t q = 0; q + 5 < P.ins.size(); q += 6) {
+    int op = P.ins[q + 4];
+    if (op == SOP_STOP) break;
+    S v[4];
+    int a = slp_arity(op);
+    for (int r = 0; r < a; ++r)
+      if (!(op == SOP_POW_INT && r == 1)) v[r] = t[P.ins[q + r]];
+    t[P.ins[q + 5]] = slp_value(op, v, P.ins[q + 1]);
+  }
+}
+// derivative of an op's output from its inputs' values v, output value c and input tangents d
+static C slp_tangent(int op, const C* v, C c, const C* d, int p) {
+  switch (op) {
+    case SOP_CB: return s_scale(v[0] * v[0], 3) * d[0];
+    case SOP_INV: return s_neg(c * c * d[0]);
+    case SOP_INV_NOT_ZERO: return s_zero(v[0]) ? d[0] : s_neg(c * c * d[0]);
+    case SOP_INVSQR: return s_neg(s_scale(c * s_inv(v[0]), 2) * d[0]);
+    case SOP_NEG: return s_neg(d[0]);
+    case SOP_SQR: return s_scale(v[0] * d[0], 2);
+    case SOP_SQRT: return s_div(d[0], s_scale(c, 2));
+    case SOP_IDENTITY: return d[0];
+    case SOP_ADD: return d[0] + d[1];
+    case SOP_DIV: return s_div(d[0] - c * d[1], v[1]);
+    case SOP_MUL: return d[0] * v[1] + v[0] * d[1];
+    case SOP_SUB: return d[0] - d[1];
+    case SOP_POW_INT: return p == 0 ? cx(0.0) : s_scale(s_pow(v[0], p - 1), p) * d[0];
+    case SOP_ADD3: return d[0] + d[1] + d[2];
+    case SOP_MUL3: return d[0] * v[1] * v[2] + v[0] * d[1] * v[2] + v[0] * v[1] * d[2];
+    case SOP_MULADD: return d[0] * v[1] + v[0] * d[1] + d[2];
+    case SOP_MULSUB: return d[0] * v[1] + v[0] * d[1] - d[2];
+    case SOP_SUBMUL: return d[2] - (d[0] * v[1] + v[0] * d[1]);
+    case SOP_ADD4: return d[0] + d[1] + d[2] + d[3];
+    case SOP_MUL4:
+      return d[0] * v[1] * v[2] * v[3] + v[0] * d[1] * v[2] * v[3] + v[0] * v[1] * d[2] * v[3] +
+             v[0] * v[1] * v[2] * d[3];
+    case SOP_MULMULADD: return d[0] * v[1] + v[0] * d[1] + d[2] * v[3] + v[2] * d[3];
+    case SOP_MULMULSUB: return d[0] * v[1] + v[0] * d[1] - (d[2] * v[3] + v[2] * d[3]);
+  }
+  return cx(0.0);
+}
+// F(x) and its Jacobian (column-major m×n), one forward-mode sweep per variable
+static void slp_eval_jac(const Slp& P, const C* x, C* u, C* U) {
+  std::vector<C> t, dt;
+  slp_tape(P, x, t);
+  for (int i = 0; i < P.n; ++i) u[i] = t[P.outputs[i]];
+  for (int j = 0; j < P.n; ++j) {
+    dt.assign(P.tape, cx(0.0));
+    dt[P.voff + j] = cx(1.0);
+    for (size_t q = 0; q + 5 < P.ins.size(); q += 6) {
+      int op = P.ins[q + 4];
+      if (op == SOP_STOP) break;
+      C v[4], d[4];
+      int a = slp_arity(op);
+      for (int r = 0; r < a; ++r)
+        if (!(op == SOP_POW_INT && r == 1)) {
+          v[r] = t[P.ins[q + r]];
+          d[r] = dt[P.ins[q + r]];
+        }
+      dt[P.ins[q + 5]] = slp_tangent(op, v, t[P.ins[q + 5]], d, P.ins[q + 1]);
+    }
+    for (int i = 0; i < P.n; ++i) U[(size_t)j * P.n + i] = dt[P.outputs[i]];
+  }
+}
+// truncated series (orders 0..K) of the ops
+static void ser_mul(const C* a, const C* b, C* c, int K) {
+  for (int k = 0; k <= K; ++k) {
+    C s = cx(0.0);
+    for (int j = 0; j <= k; ++j) s = s + a[j] * b[k - j];
+    c[k] = s;
+  }
+}
+static void ser_inv(const C* a, C* c, int K) {  // c_0 = 1/a_0, c_k = -(Σ_{j≥1} a_j c_{k-j}) c_0
+  c[0] = s_inv(a[0]);
+  for (int k = 1; k <= K; ++k) {
+    C s = cx(0.0);
+    for (int j = 1; j <= k; ++j) s = s + a[j] * c[k - j];
+    c[k] = s_neg(s) * c[0];
+  }
+}
+static void ser_pow(const C* a, int p, C* c, int K) {
+  int q = p < 0 ? -p : p;
+  std::vector<C> r(K + 1, cx(0.0)), b(a, a + K + 1), tmp(K + 1);
+  r[0] = cx(1.0);
+  while (q) {
+    if (q & 1) {
+      ser_mul(r.data(), b.data(), tmp.data(), K);
+      r = tmp;
+    }
+    q >>= 1;
+    if (q) {
+      ser_mul(b.data(), b.data(), tmp.data(), K);
+      b = tmp;
+    }
+  }
+  if (p < 0)
+    ser_inv(r.data(), c, K);
+  else
+    for (int k = 0; k <= K; ++k) c[k] = r[k];
+}
+static void slp_taylor(const Slp& P, int K, const C* tx, int nx, C* dv) {
+  const int L = K + 1, n = P.n;
+  std::vector<C> t((size_t)P.tape * L, cx(0.0));
+  auto at = [&](int slot) { return &t[(size_t)slot * L]; };
+  for (int k = 0; k < P.nconst; ++k) at(k)[0] = P.consts[k];
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < L; ++k) at(P.voff + j)[k] = k < nx ? tx[(size_t)k * n + j] : cx(0.0);
+  std::vector<C> a(L), b(L), c(L), e(L);
+  for (size_t q = 0; q + 5 < P.ins.size(); q += 6) {
+    int op = P.ins[q + 4];
+    if (op == SOP_STOP) break;
+    const C* v[4] = {nullptr, nullptr, nullptr, nullptr};
+    int ar = slp_arity(op);
+    for (int r = 0; r < ar; ++r)
+      if (!(op == SOP_POW_INT && r == 1)) v[r] = at(P.ins[q + r]);
+    C* o = at(P.ins[q + 5]);
+    auto add = [&](const C* x, const C* y, C* z, double sy) {
+      for (int k = 0; k < L; ++k) z[k] = x[k] + y[k] * sy;
+    };
+    switch (op) {
+      case SOP_IDENTITY: for (int k = 0; k < L; ++k) o[k] = v[0][k]; break;
+      case SOP_NEG: for (int k = 0; k < L; ++k) o[k] = s_neg(v[0][k]); break;
+      case SOP_ADD: add(v[0], v[1], o, 1.0); break;
+      case SOP_SUB: add(v[0], v[1], o, -1.0); break;
+      case SOP_MUL: ser_mul(v[0], v[1], o, K); break;
+      case SOP_SQR: ser_mul(v[0], v[0], o, K); break;
+      case SOP_CB: ser_mul(v[0], v[0], a.data(), K); ser_mul(a.data(), v[0], o, K); break;
+      case SOP_INV: ser_inv(v[0], o, K); break;
+      case SOP_INV_NOT_ZERO:
+        if (s_zero(v[0][0])) for (int k = 0; k < L; ++k) o[k] = v[0][k];
+        else ser_inv(v[0], o, K);
+        break;
+      case SOP_INVSQR: ser_inv(v[0], a.data(), K); ser_mul(a.data(), a.data(), o, K); break;
+      case SOP_POW_INT: ser_pow(v[0], P.ins[q + 1], o, K); break;
+      case SOP_DIV:  // c_0 = a_0/b_0, c_k = (a_k - Σ_{j≥1} b_j c_{k-j}) / b_0
+        o[0] = s_div(v[0][0], v[1][0]);
+        for (int k = 1; k <= K; ++k) {
+          C s = v[0][k];
+          for (int j = 1; j <= k; ++j) s = s - v[1][j] * o[k - j];
+          o[k] = s_div(s, v[1][0]);
+        }
+        break;
+      case SOP_SQRT:  // c_0 = √a_0, c_k = (a_k - Σ_{j=1..k-1} c_j c_{k-j}) / (2 c_0)
+        o[0] = s_sqrt(v[0][0]);
+        for (int k = 1; k <= K; ++k) {
+          C s = v[0][k];
+          for (int j = 1; j <= k - 1; ++j) s = s - o[j] * o[k - j];
+          o[k] = s_div(s, s_scale(o[0], 2));
+        }
+        break;
+      case SOP_ADD3: add(v[0], v[1], a.data(), 1.0); add(a.data(), v[2], o, 1.0); break;
+      case SOP_MUL3: ser_mul(v[0], v[1], a.data(), K); ser_mul(a.data(), v[2], o, K); break;
+      case SOP_MULADD: ser_mul(v[0], v[1], a.data(), K); add(a.data(), v[2], o, 1.0); break;
+      case SOP_MULSUB: ser_mul(v[0], v[1], a.data(), K); add(a.data(), v[2], o, -1.0); break;
+      case SOP_SUBMUL: ser_mul(v[0], v[1], a.data(), K); add(v[2], a.data(), o, -1.0); break;
+      case SOP_ADD4:
+        add(v[0], v[1], a.data(), 1.0); add(a.data(), v[2], b.data(), 1.0); add(b.data(), v[3], o, 1.0);
+        break;
+      case SOP_MUL4:
+        ser_mul(v[0], v[1], a.data(), K); ser_mul(a.data(), v[2], b.data(), K); ser_mul(b.data(), v[3], o, K);
+        break;
+      case SOP_MULMULADD: ser_mul(v[0], v[1], a.data(), K); ser_mul(v[2], v[3], b.data(), K); add(a.data(), b.data(), o, 1.0); break;
+      case SOP_MULMULSUB: ser_mul(v[0], v[1], a.data(), K); ser_mul(v[2], v[3], b.data(), K); add(a.data(), b.data(), o, -1.0); break;
+    }
+  }
+  for (int k = 0; k < L; ++k)
+    for (int i = 0; i < n; ++i) dv[(size_t)k * n + i] = at(P.outputs[i])[k];
 }
 
 // power table pw[j*(D+1)+k] = x_j^k
@@ -227,6 +507,12 @@ static void power_table(const System& F, const S* x, std::vector<S>& pw) {
 // F(x) in arithmetic S (C or CDD)
 template <class S>
 static void sys_eval(const System& F, const S* x, S* u) {
+  if (F.slp) {
+    std::vector<S> t;
+    slp_tape(*F.slp, x, t);
+    for (int i = 0; i < F.m; ++i) u[i] = t[F.slp->outputs[i]];
+    return;
+  }
   std::vector<S> pw;
   power_table(F, x, pw);
   int D = F.maxdeg;
@@ -241,6 +527,7 @@ static void sys_eval(const System& F, const S* x, S* u) {
 
 // F(x) and its Jacobian U (column-major m×n)
 static void sys_eval_jac(const System& F, const C* x, C* u, C* U) {
+  if (F.slp) return slp_eval_jac(*F.slp, x, u, U);
   std::vector<C> pw;
   power_table(F, x, pw);
   int D = F.maxdeg;
@@ -274,6 +561,7 @@ static void series_mul(const C* a, const C* b, C* c, int K) {
   }
 }
 static void sys_taylor(const System& F, int K, const C* tx, int nx, C* dv /* (K+1)×m */) {
+  if (F.slp) return slp_taylor(*F.slp, K, tx, nx, dv);
   int n = F.n, D = F.maxdeg, L = K + 1;
   std::vector<C> ps((size_t)n * (D + 1) * L, cx(0.0));
   std::vector<C> tmp(L);
@@ -1566,6 +1854,8 @@ static bool tracker_step_impl(Tracker& T);
 static thread_local std::vector<double>* tl_trace = nullptr;
 static thread_local const long* tl_trace_eg = nullptr;
 static int64_t g_trace_path = -1;  // 0-based path index to trace (-1: none)
+static Slp g_slp;  // program of F for hco_track (hco_set_slp)
+static bool g_slp_on = false;
 static std::vector<double> g_trace;
 
 // :851-926
@@ -2208,6 +2498,10 @@ int hco_track(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const d
   H.m = n;
   H.G = make_system(n, n, nG, G_eq, G_exps, G_coef);
   H.F = make_system(n, n, nF, F_eq, F_exps, F_coef);
+  if (g_slp_on) {
+    if (g_slp.n != n) return 1;
+    H.F.slp = &g_slp;
+  }
   H.gamma = C{gamma_re, gamma_im};
   TrackerOptions to;
   EndgameOptions eo;
@@ -2462,6 +2756,26 @@ int hco_homotopy_eval(int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
     out[2 * i + 1] = u[i].im;
   }
   return 0;
+}
+
+// F as a straight-line program for the following hco_track calls (instr: 6 ints per
+// instruction — input[0..3], op, output; consts re/im; tape layout as in include/hcgpu.h's
+// hc_slp); ninstr < 0 switches back to term tables.
+void hco_set_slp(int n, int ninstr, const int32_t* instr, int nconst, const double* consts, int voff, int tape,
+                 const int32_t* outputs) {
+  if (ninstr < 0) {
+    g_slp_on = false;
+    return;
+  }
+  g_slp = Slp();
+  g_slp.n = n;
+  g_slp.voff = voff;
+  g_slp.tape = tape;
+  g_slp.nconst = nconst;
+  g_slp.ins.assign(instr, instr + 6 * (size_t)ninstr);
+  for (int k = 0; k < nconst; ++k) g_slp.consts.push_back(C{consts[2 * k], consts[2 * k + 1]});
+  g_slp.outputs.assign(outputs, outputs + n);
+  g_slp_on = true;
 }
 
 // Step trace of one path of the next hco_track call (path: 0-based index, -1 = off); the

@@ -203,6 +203,43 @@ def track_toric(F_terms, weights, starts, rows, t1, t0, omega=None, mu=None, opt
     return res, xs
 
 
+def set_slp(program=None):
+    """Evaluate F as the straight-line program ``program`` (hcgpu.slp.Program) in the following
+    track() calls; None switches back to term tables."""
+    L = lib()
+    L.hco_set_slp.argtypes = [ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int,
+                              ct.c_void_p]
+    if program is None:
+        L.hco_set_slp(0, -1, None, 0, None, 0, 0, None)
+        return
+    ins, consts, voff, tape, outs = program.arrays()
+    flat = np.ascontiguousarray(np.column_stack([ins["input"], ins["op"], ins["output"]]).astype(np.int32))
+    consts = np.ascontiguousarray(consts if consts.size else np.zeros(2))
+    outs = np.ascontiguousarray(outs, dtype=np.int32)
+    L.hco_set_slp(program.n, len(ins), _ptr(flat), len(consts) // 2 if len(program._tape.consts) else 0,
+                  _ptr(consts), voff, tape, _ptr(outs))
+
+
+def track_slp(program, gamma, starts, **kw):
+    """track() of γ t G + (1 - t) F with F = program and G_i = s_i (x_i^{D_i} - 1) from the
+    program's degrees and scalings."""
+    n = program.n
+    eq, ex, cf = [], [], []
+    for i, (d, sc) in enumerate(zip(program.degrees, program.scaling)):
+        e = [0] * n
+        e[i] = int(d)
+        eq += [i, i]
+        ex += [e, [0] * n]
+        cf += [sc, -sc]
+    G = (np.asarray(eq, np.int32), np.asarray(ex, np.int32).reshape(-1, n), np.asarray(cf, np.complex128))
+    F = (np.zeros(0, np.int32), np.zeros((0, n), np.int32), np.zeros(0, np.complex128))
+    set_slp(program)
+    try:
+        return track(G, F, gamma, starts, **kw)
+    finally:
+        set_slp(None)
+
+
 TRACE_FIELDS = ["t_re", "t_im", "ds", "tau", "omega", "mu", "accepted", "iters", "norm_x", "ds_next",
                 "omega_after", "accuracy", "extended_prec", "code", "steps_eg"]
 

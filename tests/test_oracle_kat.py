@@ -254,3 +254,39 @@ def test_at_infinity_decision_depends_on_step_parameters():
     assert code(22314)[0] == "at_infinity"
     c, sing, nx = code(22314, **fast)
     assert (c, sing) == ("success", True) and nx > 1e10
+
+
+@pytest.mark.parametrize("d", [2, 6])
+def test_x_minus_10_power_as_program(d):
+    # test/endgame_test.jl:47-52: count(r -> r.winding_number == d, res) == d. The reference
+    # evaluates (x-10)^d as written; the oracle does the same through its program interpreter
+    # (the expanded polynomial's residual is rounding noise near the 6-fold root)
+    import math
+
+    from hcgpu import slp
+
+    (x,) = slp.variables(1)
+    scale = max(float(math.comb(d, k)) * 10.0 ** (d - k) for k in range(d + 1))
+    P = slp.Program([(x - 10.0) ** d], degrees=[d], scaling=[scale])
+    for k in range(3):
+        res, xs, _, _ = hco.track_slp(P, np.exp(2j * np.pi * (0.05 + k / 3)), hc.total_degree_start_solutions([d]))
+        assert list(res["winding_number"]) == [d] * d
+        assert (res["return_code"] == 1).all() and (res["singular"] == 1).all()
+        assert np.abs(xs[:, 0] - 10).max() < 1e-6
+
+
+def test_program_interpreter_matches_term_tables():
+    # the oracle's straight-line-program evaluation (values, Jacobian, Taylor series) tracks the
+    # structured systems to the endpoints its term-table evaluation of their expansions finds
+    from hcgpu import slp
+
+    for P, S in (slp.products_of_linear_forms(4, 3, 1), slp.determinantal(3, 3, 2), slp.disguised_ops(0)):
+        P.scaling = [float(np.max(np.abs(c))) for c in S.coefficients]
+        g = np.exp(2j * np.pi * 0.17)
+        H = hc.total_degree_homotopy(S, g)
+        starts = hc.total_degree_start_solutions(H.degrees)
+        ro, xo, _, _ = track(H, starts)
+        rp, xp, _, _ = hco.track_slp(P, g, starts)
+        assert np.array_equal(ro["return_code"], rp["return_code"])
+        ok = (ro["return_code"] == 1) & (ro["singular"] == 0)
+        assert (np.abs(xp[ok] - xo[ok]).max(1) / np.abs(xo[ok]).max(1)).max() <= 1e-10

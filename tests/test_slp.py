@@ -1,9 +1,11 @@
 """Systems given as straight-line programs (hc_set_slp): the program is turned into CUDA C and
-compiled by NVRTC with the tracking kernel. The CPU oracle tracks the same system from its
-expanded term table, so the check is independent of the generated code: identical return
-codes per path and nonsingular endpoints within 1e-10 relative, in FP64 and mixed precision.
+compiled by NVRTC with the tracking kernel. The CPU oracle tracks the same system twice — from
+its expanded term table (independent of the program) and through its own program interpreter —
+and both must give the GPU's return code on every path and nonsingular endpoints within 1e-10
+relative, in FP64 and mixed precision.
 The structured systems are passed unexpanded (products of linear forms; determinants by
 elimination, with divisions); one system exercises every supported op."""
+import math
 import time
 
 import numpy as np
@@ -29,6 +31,12 @@ def _check(P, S, gamma, precision, step_control="plain"):
     ok = (ro["return_code"] == 1) & (ro["singular"] == 0)
     assert ok.sum() > 0
     assert rel_err(xg[ok], xo[ok]).max() <= REL_TOL
+    # and the oracle evaluating the same program (its interpreter), path by path
+    import hco
+
+    rp, xp, _, _ = hco.track_slp(P, gamma, starts)
+    assert np.array_equal(rp["return_code"], rg["return_code"])
+    assert rel_err(xg[ok], xp[ok]).max() <= REL_TOL
     return ro, rg, T
 
 
@@ -78,3 +86,31 @@ def test_compiled_program_is_cached():
     assert time.perf_counter() - t < 2.0
     r, x, _, _ = T.track_arrays(hc.total_degree_start_solutions(P.degrees))
     assert (r["return_code"] == 1).sum() > 0
+
+
+@pytest.mark.parametrize("d", [2, 6])
+def test_reference_kat_x_minus_10_power_unexpanded(d):
+    """test/endgame_test.jl:47-52: every path of (x-10)^d ends with winding number d. The
+    reference evaluates (x-10)^d as written (ModelKit's program: a subtraction and a power);
+    expanded into a term table, the residual near x = 10 is rounding noise below |x-10| ≈ 0.04
+    for d = 6 (binomial coefficients up to 10^6), and no endgame can resolve the root. As a
+    straight-line program it passes, in both precisions, for several γ."""
+    (x,) = slp.variables(1)
+    # the start system's scaling the reference computes from the expanded support (total_degree.jl:62)
+    scale = max(float(math.comb(d, k)) * 10.0 ** (d - k) for k in range(d + 1))
+    P = slp.Program([(x - 10.0) ** d], degrees=[d], scaling=[scale])
+    import hco
+
+    for precision in ("fp64", "mixed"):
+        for k in range(3):
+            g = np.exp(2j * np.pi * (0.05 + k / 3))
+            starts = hc.total_degree_start_solutions([d])
+            T = hc.EndgameTracker(slp.slp_homotopy(P, g), hc.TrackerOptions(precision=precision))
+            r, xs, _, _ = T.track_arrays(starts)
+            assert list(r["winding_number"]) == [d] * d, (precision, k, list(r["winding_number"]))
+            assert (r["return_code"] == 1).all() and (r["singular"] == 1).all()
+            assert np.abs(xs[:, 0] - 10).max() < 1e-6
+            # the oracle evaluating the same program: same codes and winding numbers
+            ro, xo, _, _ = hco.track_slp(P, g, starts)
+            assert np.array_equal(ro["return_code"], r["return_code"])
+            assert np.array_equal(ro["winding_number"], r["winding_number"])
