@@ -550,9 +550,11 @@ int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling,
         return HC_ERR_INVALID_ARG;
       }
     }
-    if (I.output < 0 || I.output >= tape || written[I.output]) {
+    // slots are written in order and may be written again (ModelKit compacts its tapes,
+    // src/model_kit/instruction_sequence.jl:354-381); constants and variables stay fixed
+    if (I.output < 0 || I.output >= tape || I.output < nc || (I.output >= voff && I.output < voff + n)) {
       err = "instruction " + std::to_string(k) + ": output slot " + std::to_string(I.output) +
-            " is out of range, a constant or variable, or written twice";
+            " is out of range or a constant or variable";
       return HC_ERR_INVALID_ARG;
     }
     written[I.output] = 1;

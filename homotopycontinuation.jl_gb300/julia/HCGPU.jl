@@ -225,22 +225,98 @@ function homotopy_handle(H, o::HCOptions)
     h[], n
 end
 
+struct HCInstruction  # hc_instruction
+    in1::Int32
+    in2::Int32
+    in3::Int32
+    in4::Int32
+    op::Int32
+    output::Int32
+end
+
+struct HCSlp  # hc_slp
+    n::Int32
+    ninstructions::Int32
+    instructions::Ptr{HCInstruction}
+    nconstants::Int32
+    constants::Ptr{Float64}
+    variables_offset::Int32
+    tape_size::Int32
+    outputs::Ptr{Int32}
+end
+
+# The reference's own program of F (src/model_kit/instruction_sequence.jl:133-254): its
+# instructions, constants and output slots with 0-based tape indices; OpType values are
+# hc_op's (include/hcgpu.h). F must have no parameters (fix them first).
+function program_arrays(F::HC.System)
+    seq = HC.ModelKit.instruction_sequence(F)
+    isempty(seq.parameters_range) || throw(ArgumentError("fix the parameters of F before passing its program"))
+    isempty(seq.constants_range) || first(seq.constants_range) == 1 ||
+        throw(ArgumentError("unexpected tape layout: constants must come first"))
+    ins = map(seq.instructions) do I
+        a = I.input
+        # POW_INT's second input is the exponent itself, kept as is
+        fix(k, v) = (I.op == HC.ModelKit.OP_POW_INT && k == 2) ? Int32(v) : Int32(v - 1)
+        HCInstruction(fix(1, a[1]), fix(2, a[2]), fix(3, a[3]), fix(4, a[4]), Int32(I.op), Int32(I.output - 1))
+    end
+    consts = Float64[]
+    for c in seq.constants
+        z = ComplexF64(c)
+        push!(consts, real(z), imag(z))
+    end
+    n = length(seq.variables_range)
+    outputs = zeros(Int32, n)
+    for (i, k) in seq.u_assignments
+        outputs[i] = Int32(k - 1)
+    end
+    (; ins, consts, nconst = length(seq.constants), voff = Int32(first(seq.variables_range) - 1),
+       tape = Int32(seq.tape_space_needed), outputs, n)
+end
+
+# a handle holding γ t G + (1 - t) F with F the reference's program (hc_set_slp); G is the
+# total-degree start system with degrees D and scalings s
+function program_handle(F::HC.System, D, s, γ, o::HCOptions)
+    A = program_arrays(F)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hc_create, libhcgpu), Cint, (Ref{HCOptions}, Ref{Ptr{Cvoid}}), Ref(o), h))
+    GC.@preserve A begin
+        P = HCSlp(A.n, length(A.ins), pointer(A.ins), A.nconst, pointer(A.consts), A.voff, A.tape, pointer(A.outputs))
+        check(ccall((:hc_set_slp, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Ref{HCSlp}, Ptr{Int32}, Ptr{Float64}, Float64, Float64),
+                    h[], Ref(P), Int32.(D), Float64.(s), real(γ), imag(γ)), h[])
+    end
+    h[], A.n
+end
+
 """
-    GPUTracker(eg::EndgameTracker; precision = 1, step_control = 0)
+    GPUTracker(eg::EndgameTracker; precision = 1, step_control = 0, program = nothing)
 
 An `AbstractPathTracker` (src/endgame_tracker.jl:8) running the reference's `EndgameTracker`
 algorithm for `eg`'s homotopy on the GPU, with `eg`'s γ, start system, `TrackerOptions` and
 `EndgameOptions`. `precision`: 0 = complex FP64, 1 = FP32 Jacobians/LU/Taylor with FP64
 residuals and decisions. `step_control`: 0 = the reference's rule, 1 = the learned proposal
-(load its network with `set_step_model!` first).
+(load its network with `set_step_model!` first). `program = F` (the `System` `eg` tracks
+towards) passes F's own instruction sequence, unexpanded, through `hc_set_slp` instead of its
+expanded term table — as the reference evaluates it, which matters where expansion loses
+accuracy (e.g. `(x - 10)^6` near its root).
 """
 mutable struct GPUTracker <: HC.AbstractPathTracker
     handle::Ptr{Cvoid}
     n::Int
     endgame_start::Float64
-    function GPUTracker(eg::HC.EndgameTracker; precision = 1, step_control = 0)
+    function GPUTracker(eg::HC.EndgameTracker; precision = 1, step_control = 0, program = nothing)
         o = hc_options(eg.tracker.options, eg.options; precision = precision, step_control = step_control)
-        h, n = homotopy_handle(eg.tracker.homotopy, o)
+        H = eg.tracker.homotopy
+        if program === nothing
+            h, n = homotopy_handle(H, o)
+        else
+            H isa HC.StraightLineHomotopy || throw(ArgumentError("a straight-line homotopy is needed"))
+            # G_i = s_i (x_i^D_i - 1): degrees from G's own terms, scalings its parameters
+            Geq, Gexp, Gcf, nG = term_tables(H.start)
+            D = [maximum(Gexp[(k-1)*nG+i] for k in 1:length(Geq) if Geq[k] == i - 1) for i in 1:nG]
+            s = [maximum(abs(Gcf[2k-1]) for k in 1:length(Geq) if Geq[k] == i - 1) for i in 1:nG]
+            h, n = program_handle(program, D, s, H.γ, o)
+        end
         T = new(h, n, eg.options.endgame_start)
         finalizer(T -> ccall((:hc_destroy, libhcgpu), Cvoid, (Ptr{Cvoid},), T.handle), T)
     end

@@ -132,9 +132,11 @@ typedef struct hc_instruction {
   int32_t output;
 } hc_instruction;
 /* The tape: slots [0, nconstants) hold the constants (complex, re/im interleaved), slots
- * [variables_offset, variables_offset + n) the variables x_1..x_n, every other slot below
- * tape_size is written by exactly one instruction, after the slots it reads (instructions in
- * order; HC_OP_STOP ends the program). outputs[i] is the slot holding F_{i+1}. */
+ * [variables_offset, variables_offset + n) the variables x_1..x_n; instructions run in order,
+ * each reading slots already written and writing any other slot below tape_size (a slot may
+ * be written again, as in ModelKit's compacted tapes); HC_OP_STOP ends the program.
+ * outputs[i] is the slot holding F_{i+1} at the end. With 1-based Julia indices this is the
+ * reference's InstructionSequence of a system without parameters, every index minus one. */
 typedef struct hc_slp {
   int32_t n;
   int32_t ninstructions;
