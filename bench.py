@@ -443,18 +443,18 @@ def main_uneven(args, torch, hc, _lib, local):
     torch.cuda.set_stream(stream)
     L = _lib.load()
 
-    unit_paths = None
+    unit_paths, staging = None, None
     tune_s = 0.0
     if args.autotune:
         t = time.perf_counter()
-        unit_paths = hc.autotune_unit_paths(Hs, hc.TrackerOptions(precision=args.precision,
-                                                                   step_control=args.step_control),
-                                            candidates=(2, 4, 8, 16, 32), sample=60)
+        unit_paths, staging = hc.autotune(Hs, hc.TrackerOptions(precision=args.precision,
+                                                                step_control=args.step_control),
+                                          candidates=(2, 4, 8, 16, 32), sample=60)
         tune_s = time.perf_counter() - t
 
     def batch(precision, step_control):
         return hc.BatchTracker(Hs, hc.TrackerOptions(precision=precision, step_control=step_control),
-                               unit_paths=unit_paths)
+                               unit_paths=unit_paths, staging=staging if precision == args.precision else None)
 
     B = batch(args.precision, args.step_control)
     S = B.start_solutions()
@@ -577,6 +577,9 @@ def main_uneven(args, torch, hc, _lib, local):
                        "ctas": stats["blocks"], "warps_per_cta": stats["warps_per_block"],
                        "unit_paths": ({str(k): int(v) for k, v in unit_paths.items()} if unit_paths
                                       else "default: one path per warp of a CTA"),
+                       "staging": ({str(k): v for k, v in staging.items()} if staging
+                                   else "default: FP64 coefficients via L1/L2, rare FP64 areas in global"
+                                   if args.precision == "mixed" else "shared"),
                        "autotune_seconds": tune_s,
                        "l2": "256 MiB buffer written between timed steps"},
             "e2e": {"value": B.total_paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(S.nbytes),

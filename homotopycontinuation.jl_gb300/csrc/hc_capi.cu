@@ -521,7 +521,20 @@ struct hc_handle {
   BatchInstance* d_binst[2] = {nullptr, nullptr};  // [precision]
   BatchUnit* d_bunits = nullptr;
   int bninst = 0, bnunits = 0;
-  int btbytes[2] = {0, 0}, bwstride = 0;
+  int btbytes[2] = {0, 0}, bwstride[2] = {0, 0};
+  size_t bunits_cap = 0;
+  // launch plan by n (hc_set_batch_launch, hc_autotune_batch): paths per work unit (0: one per
+  // warp of a CTA) and the staging of mixed-precision instances (0/2: FP64 value coefficients via
+  // L1/L2 and the rare FP64 areas in d_bcold; 1: every table in shared memory)
+  int32_t bunit_paths[33] = {0};
+  int32_t bstaging[33] = {0};
+  // host copies of every instance's tables for re-planning: [0] FP64, [1] mixed with everything
+  // in shared memory, [2] mixed with global slices; estimated cost of one path
+  std::vector<BatchInstance> bhost[3];
+  std::vector<double> bcost;
+  int bcold = 0;  // bytes per warp of the mixed batch's global slices (0: none)
+  char* d_bcold = nullptr;
+  size_t bcold_cap = 0;
   int64_t btotal_paths = 0, btotal_vec = 0;
   // CUDA graph of the batch launch, re-recorded when its key changes
   cudaGraphExec_t bgraph = nullptr;
@@ -717,6 +730,7 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_binst[0]);
   cudaFree(h->d_binst[1]);
   cudaFree(h->d_bunits);
+  cudaFree(h->d_bcold);
   cudaFree(h->d_plist);
   cudaFree(h->d_runits);
   cudaFree(h->d_tor_w);
@@ -1320,6 +1334,99 @@ int hc_set_step_model(hc_handle* h, const float* params, const float* mean, cons
 }
 
 // ---------------------------------------------------------------------------- batches
+}  // extern "C"
+
+// Mixed-precision instance tables with the staging `staging[n]` per n. Instances with global
+// slices share one slice stride (the largest), so the warps of CTAs on different instances
+// never overlap.
+static void mixed_instances(const hc_handle* h, const int32_t* staging, std::vector<BatchInstance>& I, int* tb,
+                            int* ws, int* cold) {
+  I.resize(h->bninst);
+  *tb = *ws = *cold = 0;
+  for (int i = 0; i < h->bninst; ++i) {
+    I[i] = h->bhost[staging[h->bn[i]] == 1 ? 1 : 2][i];
+    *tb = std::max(*tb, I[i].T.bytes);
+    *ws = std::max(*ws, I[i].L.bytes);
+    *cold = std::max(*cold, I[i].L.cold);
+  }
+  for (auto& B : I)
+    if (B.L.cold > 0) B.L.cold = *cold;
+}
+
+// Work units of the instances in `which` (every instance when null): at most unit_paths[n]
+// paths of one instance (0: `wpc`, one path per warp of a CTA — measured fastest on 2,000
+// uneven instances, since small units leave little idle time at the end of a unit, when a
+// CTA's warps wait for its slowest path before the tables are re-staged), largest estimated
+// cost first.
+static std::vector<BatchUnit> batch_units(const hc_handle* h, const int32_t* unit_paths, int wpc,
+                                          const std::vector<int>* which) {
+  struct U {
+    BatchUnit u;
+    double cost;
+  };
+  std::vector<U> units;
+  auto add = [&](int i) {
+    int64_t up = unit_paths[h->bn[i]] > 0 ? unit_paths[h->bn[i]] : wpc;
+    for (int64_t lo = 0; lo < h->bnpaths[i]; lo += up) {
+      int64_t hi = std::min<int64_t>(h->bnpaths[i], lo + up);
+      units.push_back({BatchUnit{i, (int)lo, (int)hi, 0}, h->bcost[i] * (double)(hi - lo)});
+    }
+  };
+  if (which)
+    for (int i : *which) add(i);
+  else
+    for (int i = 0; i < h->bninst; ++i) add(i);
+  std::stable_sort(units.begin(), units.end(), [](const U& a, const U& b) { return a.cost > b.cost; });
+  std::vector<BatchUnit> out(units.size());
+  for (size_t k = 0; k < units.size(); ++k) out[k] = units[k].u;
+  return out;
+}
+
+// warps per CTA the default unit size assumes (shared-memory fit of the mixed tables, at most 8)
+static int batch_wpc_estimate(int tb, int ws) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(8, (227 * 1024 - HC_LAUNCH_SMEM - tb) / std::max(ws, 1)));
+}
+
+// upload `units` into a device array of the handle (grown on demand)
+static int upload_units(hc_handle* h, BatchUnit** d, size_t* cap, const std::vector<BatchUnit>& units) {
+  if (*cap < units.size() || !*d) {
+    CK(cudaStreamSynchronize(h->stream));
+    cudaFree(*d);
+    *d = nullptr;
+    *cap = 0;
+    size_t c = std::max<size_t>(1, units.size());
+    CK(cudaMalloc(d, c * sizeof(BatchUnit)));
+    *cap = c;
+  }
+  if (!units.empty())
+    CK(cudaMemcpyAsync(*d, units.data(), units.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice, h->stream));
+  return HC_OK;
+}
+
+// Make (unit_paths, staging) the batch's launch plan: mixed instance tables, queue of units.
+static int apply_batch_plan(hc_handle* h, const int32_t* unit_paths, const int32_t* staging) {
+  std::vector<BatchInstance> I1;
+  int tb = 0, ws = 0, cold = 0;
+  mixed_instances(h, staging, I1, &tb, &ws, &cold);
+  std::vector<BatchUnit> units = batch_units(h, unit_paths, batch_wpc_estimate(tb, ws), nullptr);
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpyAsync(h->d_binst[1], I1.data(), I1.size() * sizeof(BatchInstance), cudaMemcpyHostToDevice,
+                     h->stream));
+  int rc = upload_units(h, &h->d_bunits, &h->bunits_cap, units);
+  if (rc != HC_OK) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  h->bnunits = (int)units.size();
+  h->btbytes[1] = tb;
+  h->bwstride[1] = ws;
+  h->bcold = cold;
+  std::memcpy(h->bunit_paths, unit_paths, sizeof(h->bunit_paths));
+  std::memcpy(h->bstaging, staging, sizeof(h->bstaging));
+  ++h->generation;
+  return HC_OK;
+}
+
+extern "C" {
+
 int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, const int32_t* unit_paths,
                  int64_t* total_paths, int64_t* total_elements) {
   if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch: null handle");
@@ -1361,10 +1468,10 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, con
     if (rcs[i] != HC_OK) return fail(h, rcs[i], "hc_set_batch: instance " + std::to_string(i) + ": " + errs[i]);
   std::vector<char> blob;
   std::vector<ProgOffsets> off(ninstances);
-  std::vector<BatchInstance> I[2];
-  I[0].resize(ninstances);
-  I[1].resize(ninstances);
-  int tb[2] = {0, 0}, ws = 0;
+  std::vector<BatchInstance> I[3];
+  for (auto& v : I) v.resize(ninstances);
+  std::vector<double> cost(ninstances);
+  int tb0 = 0, ws0 = 0;
   int64_t tp = 0, tv = 0;
   for (int i = 0; i < ninstances; ++i) {
     WarpLayout L = make_warp_layout(P[i]);
@@ -1373,42 +1480,22 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, con
       return fail(h, HC_ERR_TOO_LARGE,
                   "hc_set_batch: instance " + std::to_string(i) + ": tables plus one path exceed shared memory");
     off[i] = pack_program(P[i], blob);
-    for (int q = 0; q < 2; ++q) {
-      BatchInstance& B = I[q][i];
-      B.T = make_table_layout(P[i], q == 0 ? HC_PREC_FP64 : HC_PREC_MIXED);
-      B.L = L;
+    for (int v = 0; v < 3; ++v) {
+      BatchInstance& B = I[v][i];
+      B.T = v == 0 ? make_table_layout(P[i], HC_PREC_FP64) : make_table_layout(P[i], HC_PREC_MIXED, v == 2);
+      B.L = v == 0 ? L : make_warp_layout(P[i], 0, v == 2);
       B.npaths = inst[i].npaths;
       B.path_off = tp;
       B.vec_off = tv;
-      tb[q] = std::max(tb[q], B.T.bytes);
     }
-    ws = std::max(ws, L.bytes);
+    tb0 = std::max(tb0, I[0][i].T.bytes);
+    ws0 = std::max(ws0, I[0][i].L.bytes);
+    // monomial evaluations, Jacobian terms and the LU of one path
+    cost[i] = (double)P[i].M * inst[i].n + (double)inst[i].n * inst[i].n * inst[i].n + (double)P[i].jcode.size();
     tp += inst[i].npaths;
     tv += inst[i].npaths * inst[i].n;
   }
-  // work units, largest estimated cost first (monomial evaluations and the LU per path)
-  int wpc_est = (int)std::max<int64_t>(1, std::min<int64_t>(8, (227 * 1024 - HC_LAUNCH_SMEM - tb[1]) / ws));
-  struct U {
-    BatchUnit u;
-    double cost;
-  };
-  std::vector<U> units;
-  for (int i = 0; i < ninstances; ++i) {
-    int n = inst[i].n;
-    // default: one path per warp of a CTA (measured fastest on 2,000 uneven instances: 8 paths
-    // per unit with 8 warps beat 16..128 by 5%; smaller units leave less idle time at the end
-    // of a unit, when a CTA's warps wait for its slowest path before the tables are re-staged)
-    int64_t up = unit_paths && unit_paths[n] > 0 ? unit_paths[n] : wpc_est;
-    double per_path = (double)P[i].M * n + (double)n * n * n + (double)P[i].jcode.size();
-    for (int64_t lo = 0; lo < inst[i].npaths; lo += up) {
-      int64_t hi = std::min<int64_t>(inst[i].npaths, lo + up);
-      units.push_back({BatchUnit{i, (int)lo, (int)hi, 0}, per_path * (double)(hi - lo)});
-    }
-  }
-  std::stable_sort(units.begin(), units.end(), [](const U& a, const U& b) { return a.cost > b.cost; });
-  std::vector<BatchUnit> hu(units.size());
-  for (size_t k = 0; k < units.size(); ++k) hu[k] = units[k].u;
-  // upload: programs, instance tables (both precisions), units
+  // upload: programs and instance tables; the launch plan (mixed tables by staging, units) follows
   h->has_batch = false;
   if (h->d_bprog_bytes < blob.size()) {
     cudaFree(h->d_bprog);
@@ -1419,29 +1506,20 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, con
   }
   for (int i = 0; i < ninstances; ++i) {
     DevProg D = bind_program(P[i], off[i], h->d_bprog, inst[i].gamma_re, inst[i].gamma_im);
-    I[0][i].P = D;
-    I[1][i].P = D;
+    for (int v = 0; v < 3; ++v) I[v][i].P = D;
   }
   for (int q = 0; q < 2; ++q) {
     cudaFree(h->d_binst[q]);
     h->d_binst[q] = nullptr;
     CK(cudaMalloc(&h->d_binst[q], (size_t)ninstances * sizeof(BatchInstance)));
   }
-  cudaFree(h->d_bunits);
-  h->d_bunits = nullptr;
-  CK(cudaMalloc(&h->d_bunits, std::max<size_t>(1, hu.size()) * sizeof(BatchUnit)));
   CK(cudaMemcpyAsync(h->d_bprog, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
-  for (int q = 0; q < 2; ++q)
-    CK(cudaMemcpyAsync(h->d_binst[q], I[q].data(), (size_t)ninstances * sizeof(BatchInstance),
-                       cudaMemcpyHostToDevice, h->stream));
-  if (!hu.empty())
-    CK(cudaMemcpyAsync(h->d_bunits, hu.data(), hu.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_binst[0], I[0].data(), (size_t)ninstances * sizeof(BatchInstance),
+                     cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   h->bninst = ninstances;
-  h->bnunits = (int)hu.size();
-  h->btbytes[0] = tb[0];
-  h->btbytes[1] = tb[1];
-  h->bwstride = ws;
+  h->btbytes[0] = tb0;
+  h->bwstride[0] = ws0;
   h->btotal_paths = tp;
   h->btotal_vec = tv;
   h->bpath_off.resize(ninstances);
@@ -1454,11 +1532,30 @@ int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* inst, con
     h->bnpaths[i] = inst[i].npaths;
     h->bn[i] = inst[i].n;
   }
+  for (int v = 0; v < 3; ++v) h->bhost[v] = std::move(I[v]);
+  h->bcost = std::move(cost);
+  int32_t up[33] = {0};
+  if (unit_paths) std::memcpy(up, unit_paths, sizeof(up));
+  int rc = apply_batch_plan(h, up, h->bstaging);
+  if (rc != HC_OK) return rc;
   h->has_batch = true;
-  ++h->generation;
   if (total_paths) *total_paths = tp;
   if (total_elements) *total_elements = tv;
   return HC_OK;
+}
+
+int hc_set_batch_launch(hc_handle* h, const int32_t* unit_paths, const int32_t* staging) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch_launch: null handle");
+  DeviceGuard dg(h);
+  if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_set_batch_launch: call hc_set_batch first");
+  int32_t up[33] = {0}, st[33] = {0};
+  for (int n = 0; n <= 32; ++n) {
+    up[n] = unit_paths ? unit_paths[n] : 0;
+    st[n] = staging ? staging[n] : 0;
+    if (up[n] < 0) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch_launch: negative unit_paths entry");
+    if (st[n] < 0 || st[n] > 2) return fail(h, HC_ERR_INVALID_ARG, "hc_set_batch_launch: staging entries must be 0, 1 or 2");
+  }
+  return apply_batch_plan(h, up, st);
 }
 
 // shared memory, warps per CTA and CTAs of a batch launch with options O
@@ -1469,12 +1566,12 @@ static int batch_geometry(hc_handle* h, const hc_options& O, int nunits, size_t*
   const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
   int wpc = O.warps_per_cta;
   if (wpc <= 0)
-    wpc = balanced_warps((int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride)),
+    wpc = balanced_warps((int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride[q])),
                          O.precision);
-  size_t smem = fixed + (size_t)wpc * h->bwstride;
+  size_t smem = fixed + (size_t)wpc * h->bwstride[q];
   while (wpc > 1 && smem > smem_cap) {
     --wpc;
-    smem = fixed + (size_t)wpc * h->bwstride;
+    smem = fixed + (size_t)wpc * h->bwstride[q];
   }
   if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "batch: working set exceeds shared memory");
   int bps = 0;
@@ -1510,8 +1607,24 @@ static BatchLaunch batch_launch(hc_handle* h, const hc_options& O, const double*
   bl.units = units;
   bl.nunits = nunits;
   bl.tbytes = h->btbytes[q];
-  bl.wstride = h->bwstride;
+  bl.wstride = h->bwstride[q];
+  la.cold = q == 1 ? h->d_bcold : nullptr;
   return bl;
+}
+
+// the mixed batch's per-warp global slices for a launch of `blocks` CTAs of `wpc` warps
+static int ensure_bcold(hc_handle* h, const hc_options& O, int blocks, int wpc) {
+  if (O.precision != HC_PREC_MIXED || h->bcold <= 0) return HC_OK;
+  size_t need = (size_t)blocks * wpc * (size_t)h->bcold;
+  if (h->bcold_cap >= need) return HC_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  cudaFree(h->d_bcold);
+  h->d_bcold = nullptr;
+  h->bcold_cap = 0;
+  CK(cudaMalloc(&h->d_bcold, need));
+  h->bcold_cap = need;
+  ++h->generation;  // a recorded graph holds the old address
+  return HC_OK;
 }
 
 int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_path_result* d_results,
@@ -1527,6 +1640,8 @@ int hc_track_batch_device(hc_handle* h, const double* d_starts, int endgame, hc_
   size_t smem = 0;
   int wpc = 0, blocks = 0;
   int rc = batch_geometry(h, h->opts, h->bnunits, &smem, &wpc, &blocks);
+  if (rc != HC_OK) return rc;
+  rc = ensure_bcold(h, h->opts, blocks, wpc);
   if (rc != HC_OK) return rc;
   h->stats_on_host = false;
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
@@ -1616,6 +1731,8 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
       int wpc = 0, blocks = 0;
       rc = batch_geometry(h, O, (int)units.size(), &smem, &wpc, &blocks);
       if (rc != HC_OK) return rc;
+      rc = ensure_bcold(h, O, blocks, wpc);
+      if (rc != HC_OK) return rc;
       BatchLaunch bl = batch_launch(h, O, (const double*)h->d_starts, endgame, h->d_res, (double*)h->d_sol,
                                     h->d_runits, (int)units.size());
       CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), h->stream));
@@ -1636,6 +1753,106 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
       if (*h->h_cancel) return stopped(h, "hc_track_batch");
     }
   }
+  return HC_OK;
+}
+
+int hc_autotune_batch(hc_handle* h, const double* starts, int sample, const int32_t* candidates, int ncandidates,
+                      int repeats, int32_t* unit_paths_out, int32_t* staging_out, double* ms_out) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_autotune_batch: null handle");
+  DeviceGuard dg(h);
+  if (!h->has_batch) return fail(h, HC_ERR_NO_SYSTEM, "hc_autotune_batch: call hc_set_batch first");
+  if (!starts || !candidates || ncandidates < 1 || ncandidates > 16 || repeats < 1)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_autotune_batch: need starts, 1..16 candidates and repeats >= 1");
+  for (int c = 0; c < ncandidates; ++c)
+    if (candidates[c] < 1) return fail(h, HC_ERR_INVALID_ARG, "hc_autotune_batch: candidates must be positive");
+  if (h->btotal_paths == 0) return HC_OK;
+  int rc = ensure_capacity_v(h, h->btotal_paths, h->btotal_vec);
+  if (rc != HC_OK) return rc;
+  start_clock(h);
+  CK(cudaMemcpyAsync(h->d_starts, starts, (size_t)h->btotal_vec * sizeof(double2), cudaMemcpyHostToDevice,
+                     h->stream));
+  const hc_options O = h->opts;
+  const bool mixed = O.precision == HC_PREC_MIXED;
+  const int nst = mixed ? 2 : 1;
+  const int32_t stval[2] = {2, 1};  // global slices, all shared
+  std::vector<int> byn[33];
+  for (int i = 0; i < h->bninst; ++i)
+    if (h->bnpaths[i] > 0 && (sample <= 0 || (int)byn[h->bn[i]].size() < sample)) byn[h->bn[i]].push_back(i);
+  int32_t up[33], st[33];
+  std::memcpy(up, h->bunit_paths, sizeof(up));
+  std::memcpy(st, h->bstaging, sizeof(st));
+  if (ms_out)
+    for (int k = 0; k < 33 * 2 * ncandidates; ++k) ms_out[k] = std::nan("");
+  cudaEvent_t ev[2];
+  CK(cudaEventCreate(&ev[0]));
+  CK(cudaEventCreate(&ev[1]));
+  auto run = [&](int n) -> int {
+    double best = INFINITY;
+    int32_t bu = up[n], bs = st[n];
+    for (int si = 0; si < nst; ++si) {
+      st[n] = mixed ? stval[si] : st[n];
+      std::vector<BatchInstance> I1;
+      int tb = 0, ws = 0, cold = 0;
+      mixed_instances(h, st, I1, &tb, &ws, &cold);
+      if (mixed) {
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaMemcpyAsync(h->d_binst[1], I1.data(), I1.size() * sizeof(BatchInstance), cudaMemcpyHostToDevice,
+                           h->stream));
+        h->btbytes[1] = tb;
+        h->bwstride[1] = ws;
+        h->bcold = cold;
+      }
+      for (int c = 0; c < ncandidates; ++c) {
+        up[n] = candidates[c];
+        std::vector<BatchUnit> units = batch_units(h, up, 0, &byn[n]);
+        int r = upload_units(h, &h->d_runits, &h->runits_cap, units);
+        if (r != HC_OK) return r;
+        size_t smem = 0;
+        int wpc = 0, blocks = 0;
+        r = batch_geometry(h, O, (int)units.size(), &smem, &wpc, &blocks);
+        if (r != HC_OK) return r;
+        r = ensure_bcold(h, O, blocks, wpc);
+        if (r != HC_OK) return r;
+        BatchLaunch bl = batch_launch(h, O, (const double*)h->d_starts, 1, h->d_res, (double*)h->d_sol,
+                                      h->d_runits, (int)units.size());
+        for (int k = 0; k <= repeats; ++k) {  // k = 0: warm-up
+          if (k == 1) CK(cudaEventRecord(ev[0], h->stream));
+          CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long),
+                             h->stream));
+          CK(launch_batch(bl, blocks, wpc, smem, h->stream));
+        }
+        CK(cudaEventRecord(ev[1], h->stream));
+        CK(wait_stream(h));
+        if (*h->h_cancel) return stopped(h, "hc_autotune_batch");
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        const double t = (double)ms / repeats;
+        if (ms_out) ms_out[(n * 2 + si) * ncandidates + c] = t;
+        if (t < best) {
+          best = t;
+          bu = up[n];
+          bs = st[n];
+        }
+      }
+    }
+    up[n] = bu;
+    st[n] = bs;
+    return HC_OK;
+  };
+  for (int n = 1; n <= 32 && rc == HC_OK; ++n)
+    if (!byn[n].empty()) rc = run(n);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (rc == HC_OK) rc = apply_batch_plan(h, up, st);
+  else {  // restore the previous plan's tables (keeping the first error)
+    int32_t pu[33], ps[33];
+    std::memcpy(pu, h->bunit_paths, sizeof(pu));
+    std::memcpy(ps, h->bstaging, sizeof(ps));
+    apply_batch_plan(h, pu, ps);
+  }
+  if (rc != HC_OK) return rc;
+  if (unit_paths_out) std::memcpy(unit_paths_out, up, sizeof(up));
+  if (staging_out) std::memcpy(staging_out, st, sizeof(st));
   return HC_OK;
 }
 

@@ -115,12 +115,12 @@ struct Stepper {
   }
 };
 
-__device__ __forceinline__ double h_fn(double a) { return 2 * a * (sqrt(4 * a * a + 1) - 2 * a); }
+static __device__ __noinline__ double h_fn(double a) { return 2 * a * (sqrt(4 * a * a + 1) - 2 * a); }
 
-__device__ __forceinline__ c64 t_to_s_plane(c64 t, int m) {  // src/predictor.jl:338-351
+static __device__ __noinline__ c64 t_to_s_plane(c64 t, int m) {  // src/predictor.jl:338-351
   double r = fast_abs(t);
   if (t.im == 0.0 && t.re > 0) return C64(nthroot(r, m));
-  double th = atan2(t.im, t.re);
+  double th = hc_atan2(t.im, t.re);
   th = fmod(th, 2 * M_PI);
   if (th < 0) th += 2 * M_PI;
   return nthroot(r, m) * cis(th / m);
@@ -336,14 +336,14 @@ struct PathTracker {
     ca = O->a;
     ch_a = h_fn(ca);
     k_sq12ha = sqrt(1 - 2 * ch_a);
-    k_a7 = pow(ca, 7.0);
+    k_a7 = hc_pow(ca, 7.0);
     double ab = O->beta_a * O->a;
     k_c1 = sqrt(1 + 2 * h_fn(ab)) - 1;
     k_hahalf = h_fn(0.5 * ab);
     k_c1half = sqrt(1 + 2 * k_hahalf) - 1;
-    k_tolacc = pow(ca, (double)((1 << O->min_newton_iters) - 1)) * ch_a;
-    k_a7h = pow(ca, 7.0) * ch_a;
-    k_a5h = pow(ca, 5.0) * ch_a;
+    k_tolacc = hc_pow(ca, (double)((1 << O->min_newton_iters) - 1)) * ch_a;
+    k_a7h = hc_pow(ca, 7.0) * ch_a;
+    k_a5h = hc_pow(ca, 5.0) * ch_a;
   }
 
   __device__ void reset_counters() {
@@ -737,10 +737,10 @@ struct PathTracker {
     if (t == tc_t) return;
     __syncwarp();
     const int T = a->L.tor_n;
-    const double lt = log(t);
+    const double lt = hc_log(t);
     for (int k = LANE; k < T; k += 32) {
       const double w = tw[k];
-      const double p = (t == 0.0) ? (w == 0.0 ? 1.0 : 0.0) : exp(w * lt);
+      const double p = (t == 0.0) ? (w == 0.0 ? 1.0 : 0.0) : hc_exp(w * lt);
       tpow[k] = p;
       tcoef[k] = vcoef64[k] * p;
     }
@@ -1441,7 +1441,7 @@ struct PathTracker {
       double Ds = fast_abs(t - pprev_t);
       // norm(x̂, x): weighted distance
       double Ds2 = Ds * Ds;
-      le0 = vnorm(ld(xhat) - xi, w) / (porder == 4 ? Ds2 * Ds2 : pow(Ds, (double)porder));
+      le0 = vnorm(ld(xhat) - xi, w) / (porder == 4 ? Ds2 * Ds2 : hc_pow(Ds, (double)porder));
     }
     predictor_compute(t, le0);
   }
@@ -1483,7 +1483,7 @@ struct PathTracker {
         pmethod = HERMITE;
         porder = 4;
         trust_region = tx_norm[0] / tx_norm[1];
-        if (isnan(local_error)) local_error = pow(tx_norm[1] / tx_norm[0], 3.0);
+        if (isnan(local_error)) local_error = hc_pow(tx_norm[1] / tx_norm[0], 3.0);
         return;
       }
       taylor_path(2, t, u);
@@ -1737,7 +1737,6 @@ struct PathTracker {
   __device__ long long ext_steps() const { return ext_accepted_steps + ext_rejected_steps; }
 
   __device__ double initial_step_size() {  // src/tracker.jl:520-539
-    double a_ = O->beta_a * O->a;
     int p = porder;
     double e = local_error;
     if (isinf(e)) e = 1e5;
@@ -1748,7 +1747,6 @@ struct PathTracker {
   }
   __device__ HC_NI void update_stepsize(const NewtonResult& res) {  // :541-588
     HC_PHASE(PH_STEPSIZE);
-    double a_ = O->beta_a * O->a;
     int p = porder;
     double om = jclamp(omega + 2 * (omega - omega_prev), omega, 8 * omega);
     double Ds;
@@ -1812,7 +1810,6 @@ struct PathTracker {
   }
   __device__ HC_NI void update_precision(double mu_low) {  // :768-786
     if (!O->extended_precision) return;
-    double a_ = O->a;
     if (extended_prec && !keep_extended_prec && !isnan(mu_low) && mu_low > mu) {
       if (mu_low * omega < k_a7h) {
         extended_prec = false;
@@ -2097,6 +2094,7 @@ struct PathTracker {
     h0 = fmaxf(h0, 0.f);
     h1 = fmaxf(h1, 0.f);
     float g0 = M->b2[u0], g1 = M->b2[u1];
+#pragma unroll 4  // fully unrolled, this once-per-step loop is 20 KB of straight-line code
     for (int v = 0; v < 64; ++v) {
       float hv = __shfl_sync(FULL, v < 32 ? h0 : h1, v & 31);
       g0 += bf(M->W2T[v * 64 + u0]) * hv;
@@ -2191,12 +2189,12 @@ struct PathTracker {
     logt2 = logt1 = dNaN();
   }
   __device__ HC_NI void valuation_update(double t) {  // :82-124
-    double logt = log(t);
+    double logt = hc_log(t);
     bool diff = wnum > 1 && !isnan(logt2);
     if (LANE < n) {
       int i = LANE;
       c64 xi = tx0[i], xdi = tx1[i], x2i = tx2[i], x3i = tx3[i];
-      double logxi = log(fast_abs(xi)), logxdi = log(fast_abs(xdi));
+      double logxi = hc_log(fast_abs(xi)), logxdi = hc_log(fast_abs(xdi));
       auto fd = [](double nu, double s, double nu2_, double s2, double nu1_, double s1_) {
         double D1 = s - s1_, D2 = s - s2, D12 = s1_ - s2;
         return (D2 * nu1_) / (D12 * D1) - ((D12 + D2) * nu2_) / (D12 * D2) - (D12 * nu) / (D1 * D2);
@@ -2372,7 +2370,7 @@ struct PathTracker {
           bool at_zero = vx[i] > 0;
           double cond_growth = kappa / aic[i];
           double coord_growth = at_zero ? aia[i] / fast_abs(x[i]) : fast_abs(x[i]) / aia[i];
-          double lim = jclamp(pow(0.25, 4 * vi), 20.0, O->min_coord_growth);
+          double lim = jclamp(hc_pow(0.25, 4 * vi), 20.0, O->min_coord_growth);
           if (coord_growth > lim && (cond_growth > O->min_cond_growth || kappa > jmax(1e8, O->min_cond))) {
             ecode = at_zero ? EC_at_zero : EC_at_infinity;
             return true;
@@ -2389,7 +2387,7 @@ struct PathTracker {
   __device__ HC_NI void add_sample(double t) {  // :630-662
     int m = eg_wnum;
     double s = nthroot(t, m);
-    double mu_ = m * pow(s, (double)(m - 1));
+    double mu_ = m * hc_pow(s, (double)(m - 1));
     double kappa = ws_cond(egrs, egcs);
     int k;
     if (singular_steps <= 2) {

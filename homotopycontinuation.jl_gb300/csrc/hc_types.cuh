@@ -61,7 +61,10 @@ __device__ __forceinline__ c32 cfms(c32 a, c32 b, c32 acc) {
   return c32{fmaf(-a.re, b.re, fmaf(a.im, b.im, acc.re)), fmaf(-a.re, b.im, fmaf(-a.im, b.re, acc.im))};
 }
 
-__device__ __forceinline__ double fast_abs(c64 a) { return sqrt(abs2(a)); }
+// Out of line (here and below): the scalar control code calls these at many sites, and one
+// copy per kernel instead of one per site keeps the code a step runs small enough for the
+// instruction cache. The results are those of the inlined forms.
+static __device__ __noinline__ double fast_abs(c64 a) { return sqrt(abs2(a)); }
 __device__ __forceinline__ double cabs(c64 a) { return hypot(a.re, a.im); }
 __device__ __forceinline__ bool isnanc(c64 a) { return isnan(a.re) || isnan(a.im); }
 __device__ __forceinline__ c64 to64(c32 a) { return c64{(double)a.re, (double)a.im}; }
@@ -79,7 +82,7 @@ __device__ __forceinline__ c32 conv<c32>(c64 a) {
 }
 
 // Smith's algorithm for a regular complex division
-__device__ __forceinline__ c64 cdiv(c64 a, c64 b) {
+static __device__ __noinline__ c64 cdiv(c64 a, c64 b) {
   if (fabs(b.re) >= fabs(b.im)) {
     if (b.re == 0.0 && b.im == 0.0) return c64{a.re / 0.0, a.im / 0.0};
     double r = b.im / b.re, den = b.re + b.im * r;
@@ -89,7 +92,7 @@ __device__ __forceinline__ c64 cdiv(c64 a, c64 b) {
     return c64{(a.re * r + a.im) / den, (a.im * r - a.re) / den};
   }
 }
-__device__ __forceinline__ c64 cis(double th) {
+static __device__ __noinline__ c64 cis(double th) {
   double s, c;
   sincos(th, &s, &c);
   return c64{c, s};
@@ -114,7 +117,11 @@ __device__ __forceinline__ double nanmin(double a, double b) {
 __device__ __forceinline__ double nanmax(double a, double b) {
   return isnan(a) ? b : (isnan(b) ? a : fmax(a, b));
 }
-__device__ __forceinline__ double nthroot(double x, int N) {  // src/utils.jl:408-422
+static __device__ __noinline__ double hc_log(double x) { return log(x); }
+static __device__ __noinline__ double hc_exp(double x) { return exp(x); }
+static __device__ __noinline__ double hc_pow(double x, double y) { return pow(x, y); }
+static __device__ __noinline__ double hc_atan2(double y, double x) { return atan2(y, x); }
+static __device__ __noinline__ double nthroot(double x, int N) {  // src/utils.jl:408-422
   if (N == 4) return sqrt(sqrt(x));
   if (N == 2) return sqrt(x);
   if (N == 3) return cbrt(x);

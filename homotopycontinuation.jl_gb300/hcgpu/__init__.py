@@ -16,7 +16,7 @@ from .systems import (
     variables,
 )
 from . import slp
-from .batch import BatchTracker, autotune_unit_paths, solve_batch
+from .batch import BatchTracker, autotune, autotune_unit_paths, solve_batch
 from .certification import CertificationResult, SolutionCertificate, certify
 from .io import read_parameters, read_solutions, write_parameters, write_solutions
 from .monodromy import MonodromyResult, find_start_pair, monodromy_solve

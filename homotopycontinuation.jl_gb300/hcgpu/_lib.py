@@ -86,7 +86,7 @@ EXPORTS = [
     "hc_track", "hc_track_device", "hc_cancel", "hc_set_time_limit", "hc_last_error", "hc_last_stats", "hc_fma_peak",
     "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc", "hc_set_step_model",
     "hc_mlp_num_params", "hc_mlp_forward", "hc_mlp_grad", "hc_mlp_adam",
-    "hc_set_slp", "hc_slp_source", "hc_set_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
+    "hc_set_slp", "hc_slp_source", "hc_set_batch", "hc_set_batch_launch", "hc_autotune_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
 ]
 STEP_LOG_FIELDS = 36
 CERT_DTYPE = np.dtype([("certified", np.int32), ("realness", np.int32), ("radius", np.float64),
@@ -136,6 +136,8 @@ def load(build_if_missing: bool = True):
     L.hc_get_step_log.argtypes = [P, P, ct.c_int64, P]
     L.hc_set_step_model.argtypes = [P, P, P, P, ct.c_double, ct.c_double]
     L.hc_set_batch.argtypes = [P, ct.c_int, P, P, P, P]
+    L.hc_set_batch_launch.argtypes = [P, P, P]
+    L.hc_autotune_batch.argtypes = [P, P, ct.c_int, P, ct.c_int, ct.c_int, P, P, P]
     L.hc_track_batch_device.argtypes = [P, P, ct.c_int, P, P, P]
     L.hc_track_batch.argtypes = [P, P, ct.c_int, P, P]
     L.hc_certify.argtypes = [P, ct.c_int64, P, ct.c_int, P, P, P]

@@ -10,6 +10,11 @@ in a CUDA graph and replayed.
     B = BatchTracker([total_degree_homotopy(F, g) for F, g in instances])
     results = B.solve()                   # list of Result, one per instance
     results = solve_batch(instances)      # the same in one call
+
+Per n, two launch parameters can be chosen (``autotune`` measures them): the paths per work
+unit, and in mixed precision the staging of the tables ("global": FP64 value coefficients
+through L1/L2 and the rare FP64 areas in per-warp global slices, more warps per CTA; "shared":
+everything in shared memory). Neither changes any result.
 """
 from __future__ import annotations
 
@@ -33,12 +38,15 @@ class InstanceDesc(ct.Structure):
                 ("gamma_re", ct.c_double), ("gamma_im", ct.c_double), ("npaths", ct.c_int64)]
 
 
+STAGING = {"global": 2, "shared": 1}
+
+
 class BatchTracker:
     """Endgame trackers of many homotopies behind one handle and one launch."""
 
     def __init__(self, homotopies: Sequence[TotalDegreeHomotopy], tracker_options: Optional[TrackerOptions] = None,
                  endgame_options: Optional[EndgameOptions] = None, npaths: Optional[Sequence[int]] = None,
-                 unit_paths: Optional[dict] = None):
+                 unit_paths: Optional[dict] = None, staging: Optional[dict] = None):
         self.homotopies = list(homotopies)
         self.tracker_options = tracker_options or TrackerOptions()
         self.options = endgame_options or EndgameOptions()
@@ -51,6 +59,7 @@ class BatchTracker:
         self.path_off = np.concatenate([[0], np.cumsum(self.npaths)])
         self.vec_off = np.concatenate([[0], np.cumsum(self.npaths * self.n)])
         self.unit_paths = dict(unit_paths or {})
+        self.staging = dict(staging or {})
         self._upload()
 
     def _upload(self):
@@ -76,10 +85,60 @@ class BatchTracker:
         _lib.check(rc, self._h.h)
         assert int(tp[0]) == int(self.path_off[-1]) and int(tv[0]) == int(self.vec_off[-1])
         self.total_paths, self.total_elements = int(tp[0]), int(tv[0])
+        self._plan()
+
+    def _plan(self):
+        up = np.zeros(33, dtype=np.int32)
+        st = np.zeros(33, dtype=np.int32)
+        for n, u in self.unit_paths.items():
+            up[int(n)] = int(u)
+        for n, v in self.staging.items():
+            if v not in STAGING:
+                raise ValueError(f"staging for n={n} must be one of {sorted(STAGING)}, got {v!r}")
+            st[int(n)] = STAGING[v]
+        P = _lib.ptr
+        _lib.check(self._h.L.hc_set_batch_launch(self._h.h, P(up), P(st)), self._h.h)
 
     def set_unit_paths(self, unit_paths: dict):
-        self.unit_paths = dict(unit_paths)
-        self._upload()
+        self.set_launch(unit_paths=unit_paths)
+
+    def set_launch(self, unit_paths: Optional[dict] = None, staging: Optional[dict] = None):
+        """Replace the per-n unit sizes and/or stagings (None keeps the current ones); the batch
+        is re-planned without recompiling (hc_set_batch_launch)."""
+        if unit_paths is not None:
+            self.unit_paths = dict(unit_paths)
+        if staging is not None:
+            self.staging = dict(staging)
+        self._plan()
+
+    def autotune(self, starts=None, candidates=(2, 4, 8, 16, 32, 64), sample=60, repeats=1):
+        """Measure and apply the fastest launch plan per n (hc_autotune_batch). Returns
+        ({n: unit_paths}, {n: staging}, {(n, staging, unit_paths): ms per launch})."""
+        if starts is None:
+            starts = self.start_solutions()
+        starts = np.ascontiguousarray(np.asarray(starts, dtype=np.complex128).reshape(-1))
+        if starts.shape[0] != self.total_elements:
+            raise ValueError(f"expected {self.total_elements} start values, got {starts.shape[0]}")
+        cand = np.asarray(candidates, dtype=np.int32)
+        up = np.zeros(33, dtype=np.int32)
+        st = np.zeros(33, dtype=np.int32)
+        ms = np.zeros(33 * 2 * len(cand), dtype=np.float64)
+        P = _lib.ptr
+        _lib.check(self._h.L.hc_autotune_batch(self._h.h, P(starts), int(sample or 0), P(cand), len(cand), repeats,
+                                               P(up), P(st), P(ms)), self._h.h)
+        mixed = self.tracker_options.precision == "mixed"
+        names = {v: k for k, v in STAGING.items()}
+        ns = sorted({int(n) for n in self.n})
+        self.unit_paths = {n: int(up[n]) for n in ns}
+        self.staging = {n: names.get(int(st[n]), "global") for n in ns} if mixed else {}
+        table = {}
+        ms = ms.reshape(33, 2, len(cand))
+        for n in ns:
+            for si, sname in enumerate(("global", "shared") if mixed else ("shared",)):
+                for ci, c in enumerate(cand):
+                    if np.isfinite(ms[n, si, ci]):
+                        table[(n, sname, int(c))] = float(ms[n, si, ci])
+        return dict(self.unit_paths), dict(self.staging), table
 
     def start_solutions(self):
         """Concatenated total-degree start solutions of every instance (src/total_degree.jl:240-262)."""
@@ -129,40 +188,30 @@ class BatchTracker:
         self._h.cancel()
 
 
-def solve_batch(instances, tracker_options=None, endgame_options=None, unit_paths=None):
+def solve_batch(instances, tracker_options=None, endgame_options=None, unit_paths=None, staging=None):
     """Solve many independent square systems by total-degree homotopies in one launch.
     ``instances``: (System, γ) pairs (as returned by systems.uneven_instances)."""
     Hs = [total_degree_homotopy(F, g) for F, g in instances]
-    return BatchTracker(Hs, tracker_options, endgame_options, unit_paths=unit_paths).solve()
+    return BatchTracker(Hs, tracker_options, endgame_options, unit_paths=unit_paths, staging=staging).solve()
+
+
+def autotune(homotopies, tracker_options=None, candidates=(2, 4, 8, 16, 32, 64), sample=None, repeats=1,
+             verbose=False):
+    """Choose the launch plan of every n of a batch of homotopies with the library's autotuner
+    (hc_autotune_batch: for each n, ``sample`` instances of that n — all when None — tracked with
+    every candidate unit size and, in mixed precision, both stagings, timed with CUDA events at
+    the full batch's launch shape). Returns ({n: unit_paths}, {n: staging}); the staging dict is
+    empty in FP64."""
+    B = BatchTracker(homotopies, tracker_options)
+    unit, staging, table = B.autotune(candidates=candidates, sample=sample, repeats=repeats)
+    if verbose:
+        for n in sorted(unit):
+            row = {f"{c}/{s}": round(t, 2) for (m, s, c), t in table.items() if m == n}
+            print(f"autotune n={n}:", row, "ms ->", (unit[n], staging.get(n, "shared")), flush=True)
+    return unit, staging
 
 
 def autotune_unit_paths(homotopies, tracker_options=None, candidates=(2, 4, 8, 16, 32, 64), sample=None,
                         repeats=1, verbose=False):
-    """Choose the paths per CTA work unit for every n in the batch: for each n, the batch of
-    that n's instances (or ``sample`` of them) is tracked with each candidate unit size and the
-    fastest is kept. Returns {n: unit_paths}."""
-    import torch
-
-    by_n = {}
-    for H in homotopies:
-        by_n.setdefault(H.n, []).append(H)
-    best = {}
-    for n, Hs in sorted(by_n.items()):
-        if sample:
-            Hs = Hs[:sample]
-        B = BatchTracker(Hs, tracker_options)
-        S = B.start_solutions()
-        times = {}
-        for c in candidates:
-            B.set_unit_paths({n: c})
-            B.track_arrays(S)  # records the graph
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(repeats):
-                B.track_arrays(S)
-            times[c] = (time.perf_counter() - t0) / repeats
-        best[n] = min(times, key=times.get)
-        if verbose:
-            print(f"autotune n={n}: {len(Hs)} instances, {B.total_paths} paths:",
-                  {c: round(t * 1e3, 2) for c, t in times.items()}, "ms ->", best[n], flush=True)
-    return best
+    """The unit sizes ``autotune`` chooses. Returns {n: unit_paths}."""
+    return autotune(homotopies, tracker_options, candidates, sample=sample, repeats=repeats, verbose=verbose)[0]

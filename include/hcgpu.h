@@ -68,7 +68,7 @@ typedef struct hc_options {
   /* GPU-side knobs (no counterpart in the reference) */
   int32_t precision;      /* enum hc_precision */
   int32_t step_control;   /* enum hc_step_control */
-  int32_t warps_per_cta;  /* 0 = autotuned */
+  int32_t warps_per_cta;  /* 0 = as many as fit in shared memory (at most 8), balanced per precision */
   int32_t ctas_per_sm;    /* 0 = as many as fit */
 } hc_options;
 
@@ -334,6 +334,27 @@ typedef struct hc_instance_desc {
  * Σ npaths_i and Σ npaths_i·n_i. */
 int hc_set_batch(hc_handle* h, int ninstances, const hc_instance_desc* instances,
                  const int32_t* unit_paths, int64_t* total_paths, int64_t* total_elements);
+/* Re-plan the current batch's launch without recompiling it, per system size n (33 entries
+ * each, indexed by n; NULL = all 0):
+ *   unit_paths[n]  paths per work unit, 0 = one per warp of a CTA;
+ *   staging[n]     mixed precision only (FP64 batches have one staging): 0 or 2 = the FP64 value
+ *                  coefficients are read through L1/L2 and the FP64 areas of the rare
+ *                  double-double and FP64 steps sit in per-warp global slices (about half the
+ *                  shared memory per warp); 1 = every table and per-warp area in shared memory.
+ * Results are identical for every plan; only the time differs. The staging also applies to
+ * later hc_set_batch calls on the handle. */
+int hc_set_batch_launch(hc_handle* h, const int32_t* unit_paths, const int32_t* staging);
+/* The launch-plan autotuner: for every n in the batch, tracks `sample` instances of that n (0 =
+ * all) from `starts` (all instances' start solutions, as hc_track_batch takes them) with each
+ * unit size in candidates[0..ncandidates-1] (1..16 entries) and, in mixed precision, each
+ * staging, times `repeats` launches after one warm-up with CUDA events on the handle's stream,
+ * and keeps the fastest. Every launch has the shape the full batch will have (tables and
+ * per-warp strides of all instances). Applies the chosen plan (hc_set_batch_launch) and writes
+ * it to unit_paths_out[33] / staging_out[33] (optional); ms_out (optional, 33·2·ncandidates)
+ * receives the milliseconds per launch, [(n·2 + s)·ncandidates + c] with s = 0 for global slices
+ * and 1 for shared staging (FP64: s = 0), NaN where nothing ran. */
+int hc_autotune_batch(hc_handle* h, const double* starts, int sample, const int32_t* candidates, int ncandidates,
+                      int repeats, int32_t* unit_paths_out, int32_t* staging_out, double* ms_out);
 /* Track every path of the batch from t=1 to t=0 (endgame != 0: EndgameTracker) on device
  * buffers; asynchronous on `stream` (NULL = the handle's stream). The launch is recorded in a
  * CUDA graph the first time a set of buffers is used and replayed afterwards. */

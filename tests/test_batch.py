@@ -59,6 +59,50 @@ def test_unit_size_and_graph_replay_do_not_change_results():
         _same(r0, x0, r2, x2)
 
 
+def test_staging_per_n_does_not_change_results():
+    """Mixed precision, each n staged in shared memory or with its FP64 areas in global slices,
+    in every combination tried: bit-identical to hc_track of each instance alone."""
+    Hs = _batch(30, seed=15, max_n=8)
+    ns = sorted({H.n for H in Hs})
+    B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed"), staging={n: "shared" for n in ns})
+    S = B.start_solutions()
+    r0, x0 = B.track_arrays(S)
+    for i, (r, x) in enumerate(B.split(r0, x0)):
+        T = hc.EndgameTracker(Hs[i], hc.TrackerOptions(precision="mixed"))
+        r1, x1, _, _ = T.track_arrays(hc.total_degree_start_solutions(Hs[i].degrees))
+        _same(r, x, r1, x1)
+    alternate = {n: ("global" if k % 2 else "shared") for k, n in enumerate(ns)}
+    for st in ({n: "global" for n in ns}, alternate):
+        B.set_launch(staging=st)
+        r2, x2 = B.track_arrays(S)
+        _same(r0, x0, r2, x2)
+        B.set_launch(unit_paths={n: 3 for n in ns})
+        r3, x3 = B.track_arrays(S)
+        _same(r0, x0, r3, x3)
+    with pytest.raises(ValueError):
+        B.set_launch(staging={ns[0]: "registers"})
+
+
+def test_autotune_picks_valid_launch_parameters():
+    """hc_autotune_batch times every (unit size, staging) pair per n, applies the fastest, and
+    the tuned batch returns the default plan's results bit for bit."""
+    Hs = _batch(16, seed=16, max_n=5)
+    ns = {H.n for H in Hs}
+    B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed"))
+    r0, x0 = B.track_arrays()
+    unit, staging, table = B.autotune(candidates=(2, 8), sample=4, repeats=1)
+    assert set(unit) == ns and set(staging) == ns
+    assert set(unit.values()) <= {2, 8} and set(staging.values()) <= {"global", "shared"}
+    assert set(table) == {(n, s, c) for n in ns for s in ("global", "shared") for c in (2, 8)}
+    assert all(t > 0 for t in table.values())
+    for n in ns:  # the chosen pair is the fastest measured one
+        assert table[(n, staging[n], unit[n])] == min(t for (m, _, _), t in table.items() if m == n)
+    r, x = B.track_arrays()
+    _same(r0, x0, r, x)
+    unit64, staging64 = hc.autotune(Hs, hc.TrackerOptions(precision="fp64"), candidates=(4,), sample=2)
+    assert set(unit64.values()) == {4} and staging64 == {}
+
+
 def test_batch_against_oracle_small_instances():
     """Instances with n ≤ 4: counts equal to the oracle's and nonsingular endpoints within 1e-10."""
     Hs = _batch(40, seed=13, max_n=4)[:12]
