@@ -565,6 +565,10 @@ struct hc_handle {
   std::string slp_src;
   SlpModule slp_mod[2];
   bool slp_built[2] = {false, false};
+  // parameter homotopy of a straight-line program (hc_set_slp_parameter_homotopy): p then q
+  int slp_np = 0;
+  double2* d_slp_pq = nullptr;
+  int slp_pq_cap = 0;
   // step log
   double* d_log = nullptr;
   unsigned long long* d_log_count = nullptr;
@@ -725,6 +729,7 @@ void hc_destroy(hc_handle* h) {
   cudaFree(h->d_last);
   cudaFree(h->d_counter);
   cudaFree(h->d_cold);
+  cudaFree(h->d_slp_pq);
   cudaFree(h->d_model);
   cudaFree(h->d_bprog);
   cudaFree(h->d_binst[0]);
@@ -792,6 +797,7 @@ int hc_set_homotopy(hc_handle* h, int n, int nG, const int32_t* G_eq, const int3
   h->has_prog = true;
   h->toric = false;
   h->slp = false;
+  h->slp_np = 0;
   return HC_OK;
 }
 
@@ -814,7 +820,7 @@ int hc_set_slp(hc_handle* h, const hc_slp* F, const int32_t* degrees, const doub
     return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp: gamma must be finite");
   SlpProgram S;
   std::string err;
-  int rc = slp_validate(F, degrees, scaling, S, err);
+  int rc = slp_validate(F, degrees, scaling, 0, 0, S, err);
   if (rc != HC_OK) return fail(h, rc, "hc_set_slp: " + err);
   const int n = S.n;
   // the start system's term table (s_i x_i^{D_i} - s_i) carries n, γ and the per-path layout;
@@ -840,20 +846,101 @@ int hc_set_slp(hc_handle* h, const hc_slp* F, const int32_t* degrees, const doub
   return rc;
 }
 
-int hc_slp_source(const hc_slp* F, const int32_t* degrees, const double* scaling, char* out, int64_t capacity,
-                  int64_t* length) {
-  SlpProgram S;
-  std::string err;
-  int rc = slp_validate(F, degrees, scaling, S, err);
-  if (rc != HC_OK) return fail(nullptr, rc, "hc_slp_source: " + err);
-  std::string src = slp_codegen(S);
+static void copy_source(const std::string& src, char* out, int64_t capacity, int64_t* length) {
   if (length) *length = (int64_t)src.size();
   if (out && capacity > 0) {
     size_t m = std::min<size_t>((size_t)capacity - 1, src.size());
     memcpy(out, src.data(), m);
     out[m] = 0;
   }
+}
+
+int hc_slp_source(const hc_slp* F, const int32_t* degrees, const double* scaling, char* out, int64_t capacity,
+                  int64_t* length) {
+  SlpProgram S;
+  std::string err;
+  int rc = slp_validate(F, degrees, scaling, 0, 0, S, err);
+  if (rc != HC_OK) return fail(nullptr, rc, "hc_slp_source: " + err);
+  copy_source(slp_codegen(S), out, capacity, length);
   return HC_OK;
+}
+
+int hc_slp_parameter_source(const hc_slp* F, int nparameters, int32_t parameters_offset, char* out,
+                            int64_t capacity, int64_t* length) {
+  if (nparameters < 1) return fail(nullptr, HC_ERR_INVALID_ARG, "hc_slp_parameter_source: need nparameters >= 1");
+  SlpProgram S;
+  std::string err;
+  int rc = slp_validate(F, nullptr, nullptr, nparameters, parameters_offset, S, err);
+  if (rc != HC_OK) return fail(nullptr, rc, "hc_slp_parameter_source: " + err);
+  copy_source(slp_codegen(S), out, capacity, length);
+  return HC_OK;
+}
+
+int hc_set_slp_parameters(hc_handle* h, const double* p, const double* q) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameters: null handle");
+  DeviceGuard dg(h);
+  if (!h->slp || h->slp_np < 1)
+    return fail(h, HC_ERR_NO_SYSTEM, "hc_set_slp_parameters: call hc_set_slp_parameter_homotopy first");
+  if (!p || !q) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameters: null parameters");
+  const int m = h->slp_np;
+  for (int k = 0; k < 2 * m; ++k)
+    if (!std::isfinite(p[k]) || !std::isfinite(q[k]))
+      return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameters: parameters must be finite");
+  std::vector<double2> pq(2 * (size_t)m);
+  for (int k = 0; k < m; ++k) {
+    pq[k] = make_double2(p[2 * k], p[2 * k + 1]);
+    pq[m + k] = make_double2(q[2 * k], q[2 * k + 1]);
+  }
+  CK(cudaStreamSynchronize(h->stream));  // a running launch reads the old values
+  if (h->slp_pq_cap < 2 * m) {
+    cudaFree(h->d_slp_pq);
+    h->d_slp_pq = nullptr;
+    h->slp_pq_cap = 0;
+    CK(cudaMalloc(&h->d_slp_pq, pq.size() * sizeof(double2)));
+    h->slp_pq_cap = 2 * m;
+    ++h->generation;
+  }
+  CK(cudaMemcpyAsync(h->d_slp_pq, pq.data(), pq.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_set_slp_parameter_homotopy(hc_handle* h, const hc_slp* F, int nparameters, int32_t parameters_offset,
+                                  const double* p, const double* q) {
+  if (!h) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameter_homotopy: null handle");
+  DeviceGuard dg(h);
+  if (nparameters < 1) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameter_homotopy: need nparameters >= 1");
+  if (!p || !q) return fail(h, HC_ERR_INVALID_ARG, "hc_set_slp_parameter_homotopy: null parameters");
+  SlpProgram S;
+  std::string err;
+  int rc = slp_validate(F, nullptr, nullptr, nparameters, parameters_offset, S, err);
+  if (rc != HC_OK) return fail(h, rc, "hc_set_slp_parameter_homotopy: " + err);
+  const int n = S.n;
+  // a placeholder term table (x_i - 1) carries n and the per-path layout; H is evaluated by the
+  // generated code alone
+  std::vector<int32_t> Geq, Gexp;
+  std::vector<double> Gcf;
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 2; ++k) {
+      Geq.push_back(i);
+      for (int j = 0; j < n; ++j) Gexp.push_back(k == 0 && j == i ? 1 : 0);
+      Gcf.push_back(k == 0 ? 1.0 : -1.0);
+      Gcf.push_back(0.0);
+    }
+  rc = hc_set_homotopy(h, n, (int)Geq.size(), Geq.data(), Gexp.data(), Gcf.data(), 0, nullptr, nullptr, nullptr,
+                       1.0, 0.0);
+  if (rc != HC_OK) return rc;
+  h->slp_src = slp_codegen(S);
+  h->slp_built[0] = h->slp_built[1] = false;
+  h->slp = true;
+  h->slp_np = nparameters;
+  rc = hc_set_slp_parameters(h, p, q);
+  if (rc == HC_OK) rc = ensure_slp(h, h->opts.precision);
+  if (rc != HC_OK) {
+    h->slp = false;
+    h->slp_np = 0;
+  }
+  return rc;
 }
 
 // handle-owned device buffers for `npaths` results and `nvec` complex vector elements
@@ -956,6 +1043,7 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   la.log_lo = h->log_lo;
   la.log_hi = h->log_hi;
   la.model = O.step_control == HC_STEP_LEARNED ? h->d_model : nullptr;
+  la.slp_pq = h->slp && h->slp_np > 0 ? h->d_slp_pq : nullptr;
   la.phase = h->d_counter + 1 + HC_NSTATS;
   la.path_list = d_path_list;
   la.path_t1 = pa.t1;
@@ -1227,6 +1315,7 @@ int hc_set_toric(hc_handle* h, int n, int nF, const int32_t* F_eq, const int32_t
   h->has_prog = true;
   h->toric = true;
   h->slp = false;
+  h->slp_np = 0;
   h->tor_rows = nrows;
   return HC_OK;
 }

@@ -123,6 +123,8 @@ struct Launch {
   const double* tor_w;
   const int32_t* tor_row;
   char* cold;  // per-warp global scratch of L.cold bytes (warp w of CTA b at (b·warps + w)·L.cold)
+  // parameter homotopy of a straight-line program: p (start parameters) then q (target)
+  const double2* slp_pq;
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

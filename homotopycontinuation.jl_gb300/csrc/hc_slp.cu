@@ -72,7 +72,7 @@ bool op_supported(int op) {
 // ---- lowered program
 enum LOp { L_ADD, L_SUB, L_MUL, L_DIV, L_NEG, L_SQR, L_INV, L_INVNZ, L_SQRT, L_POWI };
 struct Ref {
-  int kind = -1;  // 0 constant, 1 variable idx, 2 temporary idx
+  int kind = -1;  // 0 constant, 1 variable idx, 2 temporary idx, 3 parameter idx
   int idx = 0;
   cplx c;
 };
@@ -104,11 +104,11 @@ cplx h_pow(cplx a, int p) {
 }
 
 struct Lowered {
-  int n = 0;
+  int n = 0, np = 0;
   std::vector<LIns> ins;    // temporaries 0..ins.size()-1
   std::vector<Ref> out;     // per equation
   std::vector<char> live;   // per temporary: reaches an output
-  std::vector<char> usedvar;
+  std::vector<char> usedvar, usedpar;
 };
 
 struct Lowerer {
@@ -186,11 +186,16 @@ struct Lowerer {
 Lowered lower(const SlpProgram& P) {
   Lowerer W;
   W.L.n = P.n;
+  W.L.np = P.np;
   std::vector<Ref> slot(P.tape);
   for (int k = 0; k < P.nconst; ++k) slot[k] = W.cst(cplx(P.consts[2 * k], P.consts[2 * k + 1]));
   for (int j = 0; j < P.n; ++j) {
     slot[P.voff + j].kind = 1;
     slot[P.voff + j].idx = j;
+  }
+  for (int k = 0; k < P.np; ++k) {
+    slot[P.poff + k].kind = 3;
+    slot[P.poff + k].idx = k;
   }
   for (const hc_instruction& I : P.instr) {
     if (I.op == HC_OP_STOP) break;
@@ -205,9 +210,11 @@ Lowered lower(const SlpProgram& P) {
   Lowered& L = W.L;
   L.live.assign(L.ins.size(), 0);
   L.usedvar.assign(P.n, 0);
+  L.usedpar.assign(P.np, 0);
   auto mark = [&](const Ref& r) {
     if (r.kind == 2) L.live[r.idx] = 1;
     if (r.kind == 1) L.usedvar[r.idx] = 1;
+    if (r.kind == 3) L.usedpar[r.idx] = 1;
   };
   for (const Ref& r : L.out) mark(r);
   for (int k = (int)L.ins.size() - 1; k >= 0; --k)
@@ -238,6 +245,7 @@ std::string emit_eval(const Lowered& L, bool tangent) {
   auto val = [&](const Ref& r) -> std::string {
     if (r.kind == 0) return kc("T", r.c);
     if (r.kind == 1) return "x" + std::to_string(r.idx);
+    if (r.kind == 3) return "p" + std::to_string(r.idx);
     return "t" + std::to_string(r.idx);
   };
   std::vector<char> hasd(L.ins.size(), 0);
@@ -246,13 +254,19 @@ std::string emit_eval(const Lowered& L, bool tangent) {
     if (r.kind == 1) return "dx" + std::to_string(r.idx);
     return "u" + std::to_string(r.idx);
   };
+  // pq: the parameter homotopy's p (entries 0..np-1) and q (np..2np-1); t: where it is
+  // evaluated (both unused without parameters)
   o << "template <class T>\n__device__ __forceinline__ void " << (tangent ? "eval_vt" : "eval_v")
-    << "(const c64* __restrict__ xv, int lane, T& Fi" << (tangent ? ", T* col" : "") << ") {\n";
+    << "(const c64* __restrict__ xv, const c64* __restrict__ pq, c64 t, int lane, T& Fi"
+    << (tangent ? ", T* col" : "") << ") {\n";
   for (int j = 0; j < n; ++j)
     if (L.usedvar[j]) {
       o << "  const T x" << j << " = var<T>(xv[" << j << "]);\n";
       if (tangent) o << "  const T dx" << j << " = unit<T>(lane == " << j << ");\n";
     }
+  for (int k = 0; k < L.np; ++k)
+    if (L.usedpar[k])
+      o << "  const T p" << k << " = var<T>(param_at(pq[" << k << "], pq[" << L.np + k << "], t));\n";
   for (size_t k = 0; k < L.ins.size(); ++k) {
     if (!L.live[k]) continue;
     const LIns& I = L.ins[k];
@@ -320,6 +334,7 @@ std::string emit_series(const Lowered& L, int K) {
   auto ser = [&](const Ref& r) -> S {
     if (r.kind == 0) return S{0, r.c, "", 0};
     if (r.kind == 1) return S{1, cplx(), "x" + std::to_string(r.idx), K - 1};
+    if (r.kind == 3) return S{1, cplx(), "p" + std::to_string(r.idx), 1};  // p(t + s) = p(t) + s (p - q)
     return tmp[r.idx];
   };
   auto at = [&](const S& s, int q) -> std::string {  // order q or "" when zero
@@ -348,11 +363,16 @@ std::string emit_series(const Lowered& L, int K) {
   };
   auto fresh = [&]() { return "h" + std::to_string(hidden++); };
   o << "__device__ __forceinline__ void series" << K
-    << "(const c64* __restrict__ tx0, const c64* __restrict__ tx1, const c64* __restrict__ tx2, int lane, c64& Flo, "
-       "c64& Fhi) {\n";
+    << "(const c64* __restrict__ tx0, const c64* __restrict__ tx1, const c64* __restrict__ tx2, "
+       "const c64* __restrict__ pq, c64 t, int lane, c64& Flo, c64& Fhi) {\n";
   for (int j = 0; j < n; ++j)
     if (L.usedvar[j])
       for (int q = 0; q < K; ++q) o << "  const c64 x" << j << "_" << q << " = tx" << q << "[" << j << "];\n";
+  for (int k = 0; k < L.np; ++k)
+    if (L.usedpar[k]) {
+      o << "  const c64 p" << k << "_0 = param_at(pq[" << k << "], pq[" << L.np + k << "], t);\n";
+      o << "  const c64 p" << k << "_1 = pq[" << k << "] - pq[" << L.np + k << "];\n";
+    }
   for (size_t k = 0; k < L.ins.size(); ++k) {
     if (!L.live[k]) continue;
     const LIns& I = L.ins[k];
@@ -476,7 +496,10 @@ std::string emit_series(const Lowered& L, int K) {
     }
     tmp[k] = r;
   }
-  const int lo = K == 1 ? 0 : K - 1, hi = K == 1 ? 0 : K;
+  // straight-line homotopy: orders K-1 and K of F (order 0 twice for K = 1: the t-derivative
+  // is γG - F); parameter homotopy: orders K-1 and K of F(x(s); p(t + s)), whose order K is
+  // the homotopy's
+  const int lo = (K == 1 && L.np == 0) ? 0 : K - 1, hi = (K == 1 && L.np == 0) ? 0 : K;
   o << "  Flo = Fhi = kc<c64>(0.0, 0.0);\n";
   for (int i = 0; i < n; ++i) {
     S s = ser(L.out[i]);
@@ -490,9 +513,14 @@ std::string emit_series(const Lowered& L, int K) {
 
 }  // namespace
 
-int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling, SlpProgram& P, std::string& err) {
-  if (!F || !degrees || !scaling) {
+int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling, int nparams, int poff,
+                 SlpProgram& P, std::string& err) {
+  if (!F || (nparams == 0 && (!degrees || !scaling))) {
     err = "null argument";
+    return HC_ERR_INVALID_ARG;
+  }
+  if (nparams < 0 || nparams > 1024) {
+    err = "need 0 <= nparameters <= 1024";
     return HC_ERR_INVALID_ARG;
   }
   const int n = F->n;
@@ -519,9 +547,15 @@ int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling,
       err = "constants must be finite";
       return HC_ERR_INVALID_ARG;
     }
-  std::vector<char> written(tape, 0);
-  for (int k = 0; k < nc; ++k) written[k] = 1;
-  for (int j = 0; j < n; ++j) written[voff + j] = 1;
+  if (nparams > 0 && (poff < nc || poff + nparams > tape || (poff < voff + n && poff + nparams > voff))) {
+    err = "parameters must occupy slots [parameters_offset, +nparameters) within the tape, apart from the "
+          "constants and variables";
+    return HC_ERR_INVALID_ARG;
+  }
+  std::vector<char> written(tape, 0), fixed(tape, 0);
+  for (int k = 0; k < nc; ++k) written[k] = fixed[k] = 1;
+  for (int j = 0; j < n; ++j) written[voff + j] = fixed[voff + j] = 1;
+  for (int k = 0; k < nparams; ++k) written[poff + k] = fixed[poff + k] = 1;
   P.instr.clear();
   for (int k = 0; k < F->ninstructions; ++k) {
     const hc_instruction& I = F->instructions[k];
@@ -551,10 +585,11 @@ int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling,
       }
     }
     // slots are written in order and may be written again (ModelKit compacts its tapes,
-    // src/model_kit/instruction_sequence.jl:354-381); constants and variables stay fixed
-    if (I.output < 0 || I.output >= tape || I.output < nc || (I.output >= voff && I.output < voff + n)) {
+    // src/model_kit/instruction_sequence.jl:354-381); constants, variables and parameters stay
+    // fixed
+    if (I.output < 0 || I.output >= tape || fixed[I.output]) {
       err = "instruction " + std::to_string(k) + ": output slot " + std::to_string(I.output) +
-            " is out of range or a constant or variable";
+            " is out of range or a constant, variable or parameter";
       return HC_ERR_INVALID_ARG;
     }
     written[I.output] = 1;
@@ -567,28 +602,37 @@ int slp_validate(const hc_slp* F, const int32_t* degrees, const double* scaling,
       return HC_ERR_INVALID_ARG;
     }
   }
-  for (int i = 0; i < n; ++i)
-    if (degrees[i] < 1 || degrees[i] > 64 || !std::isfinite(scaling[i])) {
-      err = "start system: degrees must lie in [1, 64] and scalings be finite";
-      return HC_ERR_INVALID_ARG;
-    }
+  if (nparams == 0)
+    for (int i = 0; i < n; ++i)
+      if (degrees[i] < 1 || degrees[i] > 64 || !std::isfinite(scaling[i])) {
+        err = "start system: degrees must lie in [1, 64] and scalings be finite";
+        return HC_ERR_INVALID_ARG;
+      }
   P.n = n;
   P.nconst = nc;
   P.voff = voff;
   P.tape = tape;
+  P.np = nparams;
+  P.poff = nparams > 0 ? poff : 0;
   P.consts.assign(F->constants, F->constants + 2 * nc);
   P.outputs.assign(F->outputs, F->outputs + n);
-  P.degrees.assign(degrees, degrees + n);
-  P.scaling.assign(scaling, scaling + n);
+  if (nparams == 0) {
+    P.degrees.assign(degrees, degrees + n);
+    P.scaling.assign(scaling, scaling + n);
+  } else {  // no start system
+    P.degrees.assign(n, 1);
+    P.scaling.assign(n, 1.0);
+  }
   return HC_OK;
 }
 
 std::string slp_codegen(const SlpProgram& P) {
   Lowered L = lower(P);
   std::ostringstream o;
-  o << "// generated from a straight-line program (n = " << P.n << ", " << P.instr.size() << " instructions, "
-    << L.ins.size() << " lowered operations)\n";
+  o << "// generated from a straight-line program (n = " << P.n << ", " << P.np << " parameters, "
+    << P.instr.size() << " instructions, " << L.ins.size() << " lowered operations)\n";
   o << "#include \"hc_slp_ops.cuh\"\nnamespace hcslp {\nconstexpr int NV = " << P.n << ";\n";
+  o << "constexpr int NP = " << P.np << ";  // > 0: parameter homotopy F(x; t p + (1 - t) q)\n";
   o << "__constant__ int slp_degree[NV] = {";
   for (int i = 0; i < P.n; ++i) o << (i ? ", " : "") << P.degrees[i];
   o << "};\n__constant__ double slp_scaling[NV] = {";

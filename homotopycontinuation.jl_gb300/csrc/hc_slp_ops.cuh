@@ -42,6 +42,15 @@ template <>
 __device__ __forceinline__ cdd var<cdd>(c64 x) {
   return hcd::cdd_of(x);
 }
+// parameter k of a parameter homotopy at t: t p + (1 - t) q (tp!,
+// src/homotopies/parameter_homotopy.jl:64-87; real t in real arithmetic, as there)
+__device__ __forceinline__ c64 param_at(c64 p, c64 q, c64 t) {
+  if (t.im == 0.0) {
+    const double s = t.re, r = 1.0 - t.re;
+    return c64{s * p.re + r * q.re, s * p.im + r * q.im};
+  }
+  return t * p + (c64{1.0, 0.0} - t) * q;
+}
 // 1 when sel, else 0 (the seed of a tangent)
 template <class T>
 __device__ __forceinline__ T unit(bool sel) {

@@ -555,14 +555,20 @@ struct PathTracker {
     G = s * (p * xi - C64(1.0));
     dG = (s * (double)D) * p;
   }
+  // parameters of a parameter homotopy (p then q), unused otherwise
+  __device__ __forceinline__ const c64* slp_pq() const { return (const c64*)a->slp_pq; }
   __device__ HC_NI void slp_H_eval(const c64* xv, c64 t, c64* out) {
     __syncwarp();
     c64 F;
-    hcslp::eval_v<c64>(xv, LANE, F);
+    hcslp::eval_v<c64>(xv, slp_pq(), t, LANE, F);
     if (LANE < n) {
-      c64 G, dG;
-      slp_start(xv[LANE], G, dG);
-      out[LANE] = (gamma() * t) * G + (C64(1.0) - t) * F;
+      if constexpr (hcslp::NP > 0) {
+        out[LANE] = F;  // H(x, t) = F(x; t p + (1 - t) q)
+      } else {
+        c64 G, dG;
+        slp_start(xv[LANE], G, dG);
+        out[LANE] = (gamma() * t) * G + (C64(1.0) - t) * F;
+      }
     }
     __syncwarp();
   }
@@ -573,23 +579,29 @@ struct PathTracker {
     __syncwarp();
     const c64 ts = gamma() * t, tt = C64(1.0) - t;
     T Fi, col[hcslp::NV];
-    hcslp::eval_vt<T>(xv, LANE, Fi, col);
+    hcslp::eval_vt<T>(xv, slp_pq(), t, LANE, Fi, col);
     c64 F64;
     if constexpr (std::is_same<T, c64>::value)
       F64 = Fi;
     else
-      hcslp::eval_v<c64>(xv, LANE, F64);
+      hcslp::eval_v<c64>(xv, slp_pq(), t, LANE, F64);
     T* A = (T*)Ab;
     if (LANE < n) {
-      c64 G, dG;
-      slp_start(xv[LANE], G, dG);
-      r[LANE] = ts * G + tt * F64;
-      const T tsT = conv<T>(ts), ttT = conv<T>(tt), dGT = conv<T>(dG);
+      if constexpr (hcslp::NP > 0) {
+        r[LANE] = F64;
 #pragma unroll
-      for (int i = 0; i < hcslp::NV; ++i) {
-        T e = ttT * col[i];
-        if (i == LANE) e = e + tsT * dGT;
-        A[LANE * n + i] = e;
+        for (int i = 0; i < hcslp::NV; ++i) A[LANE * n + i] = col[i];
+      } else {
+        c64 G, dG;
+        slp_start(xv[LANE], G, dG);
+        r[LANE] = ts * G + tt * F64;
+        const T tsT = conv<T>(ts), ttT = conv<T>(tt), dGT = conv<T>(dG);
+#pragma unroll
+        for (int i = 0; i < hcslp::NV; ++i) {
+          T e = ttT * col[i];
+          if (i == LANE) e = e + tsT * dGT;
+          A[LANE * n + i] = e;
+        }
       }
     }
     __syncwarp();
@@ -597,25 +609,35 @@ struct PathTracker {
   __device__ HC_NI void slp_H_eval_dd(const c64* xv, c64 t, c64* out) {
     __syncwarp();
     cdd F;
-    hcslp::eval_v<cdd>(xv, LANE, F);
+    hcslp::eval_v<cdd>(xv, slp_pq(), t, LANE, F);
     if (LANE < n) {
-      const cdd s = cdd_of(C64(hcslp::slp_scaling[LANE]));
-      const cdd G = s * hcslp::spow(cdd_of(xv[LANE]), hcslp::slp_degree[LANE]) - s;
-      const cdd ts = cdd_of(gamma() * t), tt = cdd_of(C64(1.0) - t);
-      out[LANE] = round_c(ts * G + tt * F);
+      if constexpr (hcslp::NP > 0) {
+        out[LANE] = round_c(F);
+      } else {
+        const cdd s = cdd_of(C64(hcslp::slp_scaling[LANE]));
+        const cdd G = s * hcslp::spow(cdd_of(xv[LANE]), hcslp::slp_degree[LANE]) - s;
+        const cdd ts = cdd_of(gamma() * t), tt = cdd_of(C64(1.0) - t);
+        out[LANE] = round_c(ts * G + tt * F);
+      }
     }
     __syncwarp();
   }
-  // taylor! (K = 1: γ G(x) - F(x); K ≥ 2: order K of H(x(s), t + s) with x(s) = Σ_{k<K} tx_k s^k)
+  // taylor!: order K of H(x(s), t + s) with x(s) = Σ_{k<K} tx_k s^k (K = 1: ∂H/∂t, for the
+  // straight-line homotopy γ G(x) - F(x))
   __device__ HC_NI void slp_H_taylor(int K, c64 t, c64* out) {
     __syncwarp();
     c64 Flo, Fhi;
     if (K == 1)
-      hcslp::series1(tx0, tx1, tx2, LANE, Flo, Fhi);
+      hcslp::series1(tx0, tx1, tx2, slp_pq(), t, LANE, Flo, Fhi);
     else if (K == 2)
-      hcslp::series2(tx0, tx1, tx2, LANE, Flo, Fhi);
+      hcslp::series2(tx0, tx1, tx2, slp_pq(), t, LANE, Flo, Fhi);
     else
-      hcslp::series3(tx0, tx1, tx2, LANE, Flo, Fhi);
+      hcslp::series3(tx0, tx1, tx2, slp_pq(), t, LANE, Flo, Fhi);
+    if constexpr (hcslp::NP > 0) {
+      if (LANE < n) out[LANE] = Fhi;  // taylor!(u, v, F, tx, tp!(H, t)) (parameter_homotopy.jl:98-101)
+      __syncwarp();
+      return;
+    }
     if (LANE < n) {
       // G_i along x_i(s): s_i (x_i(s)^D - 1), four orders by repeated truncated products
       const c64 z = C64(0.0);

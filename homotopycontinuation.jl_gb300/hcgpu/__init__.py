@@ -20,7 +20,7 @@ from .batch import BatchTracker, autotune, autotune_unit_paths, solve_batch
 from .certification import CertificationResult, SolutionCertificate, certify
 from .io import read_parameters, read_solutions, write_parameters, write_solutions
 from .monodromy import MonodromyResult, find_start_pair, monodromy_solve
-from .parameters import FiniteException, ParameterHomotopy, ParametricSystem, parameter_homotopy
+from .parameters import FiniteException, ParameterHomotopy, ParametricSystem, parameter_homotopy, parametric_system
 from .polyhedral_homotopy import (MixedCell, PolyhedralStartSolutions, PolyhedralTracker, fine_mixed_cells, mixed_volume,
                          paths_to_track, polyhedral, solve_binomial)
 from .tracking import (

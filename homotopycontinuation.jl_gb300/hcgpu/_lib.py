@@ -86,7 +86,7 @@ EXPORTS = [
     "hc_track", "hc_track_device", "hc_cancel", "hc_set_time_limit", "hc_last_error", "hc_last_stats", "hc_fma_peak",
     "hc_set_step_log", "hc_get_step_log", "hc_track_noalloc", "hc_set_step_model",
     "hc_mlp_num_params", "hc_mlp_forward", "hc_mlp_grad", "hc_mlp_adam",
-    "hc_set_slp", "hc_slp_source", "hc_set_batch", "hc_set_batch_launch", "hc_autotune_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
+    "hc_set_slp", "hc_slp_source", "hc_set_slp_parameter_homotopy", "hc_set_slp_parameters", "hc_slp_parameter_source", "hc_set_batch", "hc_set_batch_launch", "hc_autotune_batch", "hc_track_batch_device", "hc_track_batch", "hc_certify", "hc_set_toric", "hc_track_toric", "hc_mixed_cells",
 ]
 STEP_LOG_FIELDS = 36
 CERT_DTYPE = np.dtype([("certified", np.int32), ("realness", np.int32), ("radius", np.float64),
@@ -122,6 +122,9 @@ def load(build_if_missing: bool = True):
     L.hc_set_homotopy.argtypes = [P, ct.c_int, ct.c_int, P, P, P, ct.c_int, P, P, P, ct.c_double, ct.c_double]
     L.hc_set_slp.argtypes = [P, P, P, P, ct.c_double, ct.c_double]
     L.hc_slp_source.argtypes = [P, P, P, P, ct.c_int64, P]
+    L.hc_set_slp_parameter_homotopy.argtypes = [P, P, ct.c_int, ct.c_int32, P, P]
+    L.hc_set_slp_parameters.argtypes = [P, P, P]
+    L.hc_slp_parameter_source.argtypes = [P, ct.c_int, ct.c_int32, P, ct.c_int64, P]
     L.hc_track.argtypes = [P, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_double,
                            P, P, P, P]
     L.hc_track_device.argtypes = [P, ct.c_int64, P, ct.c_int, ct.c_double, ct.c_double, ct.c_double,

@@ -47,19 +47,24 @@ class BatchTracker:
     def __init__(self, homotopies: Sequence[TotalDegreeHomotopy], tracker_options: Optional[TrackerOptions] = None,
                  endgame_options: Optional[EndgameOptions] = None, npaths: Optional[Sequence[int]] = None,
                  unit_paths: Optional[dict] = None, staging: Optional[dict] = None):
-        self.homotopies = list(homotopies)
         self.tracker_options = tracker_options or TrackerOptions()
         self.options = endgame_options or EndgameOptions()
         self._h = _Handle(make_options(self.tracker_options, self.options))
         self._h.setup_step_control(self.tracker_options)
+        self.unit_paths = dict(unit_paths or {})
+        self.staging = dict(staging or {})
+        self.set_homotopies(homotopies, npaths)
+
+    def set_homotopies(self, homotopies: Sequence[TotalDegreeHomotopy], npaths: Optional[Sequence[int]] = None):
+        """Replace the batch (hc_set_batch again) on the same handle: options, step model and
+        device buffers are kept (monodromy's edges, parameter targets)."""
+        self.homotopies = list(homotopies)
         if npaths is None:
             npaths = [int(np.prod(H.degrees)) for H in self.homotopies]
         self.npaths = np.asarray(npaths, dtype=np.int64)
         self.n = np.array([H.n for H in self.homotopies], dtype=np.int64)
         self.path_off = np.concatenate([[0], np.cumsum(self.npaths)])
         self.vec_off = np.concatenate([[0], np.cumsum(self.npaths * self.n)])
-        self.unit_paths = dict(unit_paths or {})
-        self.staging = dict(staging or {})
         self._upload()
 
     def _upload(self):

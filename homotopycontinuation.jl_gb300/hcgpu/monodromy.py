@@ -136,6 +136,7 @@ def monodromy_solve(F: ParametricSystem, sols=None, p=None, *, seed: Optional[in
     loops = rounds = tracked = 0
     history = []
     code = "heuristic_stop"
+    B = None  # one batch tracker (handle, buffers, step model) for every edge
     while True:
         if target_solutions_count is not None and len(U) >= target_solutions_count:
             code = "success"
@@ -154,7 +155,10 @@ def monodromy_solve(F: ParametricSystem, sols=None, p=None, *, seed: Optional[in
             if not alive:
                 break
             Hs = [ParameterHomotopy(F, legs[i][e], legs[i][e + 1]) for i in alive]
-            B = BatchTracker(Hs, to, eo, npaths=[len(current[i]) for i in alive])
+            if B is None:
+                B = BatchTracker(Hs, to, eo, npaths=[len(current[i]) for i in alive])
+            else:
+                B.set_homotopies(Hs, npaths=[len(current[i]) for i in alive])
             res, sol = B.track_arrays(np.concatenate([current[i].reshape(-1) for i in alive]))
             tracked += B.total_paths
             for (r, x), i in zip(B.split(res, sol), alive):

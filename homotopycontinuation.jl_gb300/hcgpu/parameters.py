@@ -10,13 +10,18 @@ common case of coefficient-parameter homotopies — this equals
     H(x, t) = t F(x; p) + (1 - t) F(x; q),
 
 which is the straight-line homotopy the GPU kernel tracks (γ t G + (1 - t) F with G = F(·; p),
-F = F(·; q), γ = 1). Systems whose coefficients depend non-linearly on the parameters are
-rejected with NotImplementedError.
+F = F(·; q), γ = 1). Any other dependence on the parameters goes through a straight-line
+program with parameters (``hcgpu.slp``): the parameters are inputs of the generated evaluator,
+computed at each t as t p + (1 - t) q, with the series p(t + s) = p(t) + s (p - q) in the
+predictor's Taylor coefficients — the reference's ParameterHomotopy itself.
+``parametric_system(polys, nvars, nparams)`` picks the form: term tables when the parameters
+enter affinely, a program otherwise.
 
 API, mirroring the reference:
 
-* ``ParametricSystem.from_polys(polys, nvars, nparams)`` — ``System(eqs, variables, parameters)``;
-  ``F(p)`` fixes the parameters (``fix_parameters``, src/systems/fixed_parameter_system.jl).
+* ``parametric_system(polys, nvars, nparams)`` — ``System(eqs, variables, parameters)``;
+  ``ParametricSystem.from_polys`` for the affine case; ``F(p)`` (``Program.fixed(p)``) fixes the
+  parameters (``fix_parameters``, src/systems/fixed_parameter_system.jl).
 * ``ParameterHomotopy(F, p, q)`` / ``parameter_homotopy(F; start_parameters, target_parameters)``
   (src/solve.jl:233-260), usable with ``Tracker`` and ``EndgameTracker``.
 * ``solve(F, starts; start_parameters, target_parameters)`` (src/solve.jl:447-526): one
@@ -71,8 +76,9 @@ class ParametricSystem:
                 dp = sum(pe)
                 if dp > 1:
                     raise NotImplementedError(
-                        "parameters must enter the coefficients affinely (a term of degree "
-                        f"{dp} in the parameters in equation {i})")
+                        "ParametricSystem holds coefficients affine in the parameters (a term of degree "
+                        f"{dp} in the parameters in equation {i}); parametric_system() returns a "
+                        "straight-line program for any other dependence")
                 c = acc.setdefault(xe, [0j, np.zeros(nparams, dtype=np.complex128)])
                 if dp == 0:
                     c[0] += v
@@ -123,9 +129,57 @@ class ParametricSystem:
         return self(p).evaluate(x)
 
 
+def parametric_system(polys: Sequence[Poly], nvars: int, nparams: int):
+    """``System(polys, variables, parameters)``: polynomials in nvars + nparams variables, the
+    first nvars the unknowns. A ParametricSystem (term tables) when the parameters enter the
+    coefficients affinely, else an ``slp.Program`` with parameters (monomials in x and p shared
+    across equations)."""
+    try:
+        return ParametricSystem.from_polys(polys, nvars, nparams)
+    except NotImplementedError:
+        pass
+    from .slp import Program, variables_and_parameters
+
+    x, p = variables_and_parameters(nvars, nparams)
+    v = list(x) + list(p)
+    cache: dict = {}
+
+    def mono(e):
+        e = tuple(int(a) for a in e)
+        if e not in cache:
+            acc = None
+            for j, k in enumerate(e):
+                if k:
+                    f = v[j] if k == 1 else v[j] ** k
+                    acc = f if acc is None else acc * f
+            cache[e] = acc
+        return cache[e]
+
+    outs, degs = [], []
+    for poly in polys:
+        if poly.nvars != nvars + nparams:
+            raise ValueError(f"expected {nvars + nparams} variables, got {poly.nvars}")
+        acc = None
+        for e, c in poly.terms.items():
+            m = mono(e)
+            term = complex(c) if m is None else (m if c == 1 else complex(c) * m)
+            acc = term if acc is None else acc + term
+        outs.append(acc if acc is not None else 0.0)
+        degs.append(max([sum(e[:nvars]) for e in poly.terms] + [1]))
+    return Program(outs, degs)
+
+
 class ParameterHomotopy:
-    """H(x,t) = F(x; t p + (1-t) q) (src/homotopies/parameter_homotopy.jl:3-44) in the
-    straight-line form the tracker runs: G = F(·; p), F = F(·; q), γ = 1."""
+    """H(x,t) = F(x; t p + (1-t) q) (src/homotopies/parameter_homotopy.jl:3-44). For a
+    ParametricSystem (affine parameters) in the straight-line form the tracker runs: G = F(·; p),
+    F = F(·; q), γ = 1; for an ``slp.Program`` with parameters, an ``SLPParameterHomotopy``."""
+
+    def __new__(cls, F, start_parameters=None, target_parameters=None):
+        from .slp import Program, SLPParameterHomotopy
+
+        if isinstance(F, Program):
+            return SLPParameterHomotopy(F, start_parameters, target_parameters)
+        return super().__new__(cls)
 
     def __init__(self, F: ParametricSystem, start_parameters, target_parameters):
         m, n = F.nequations, F.n
@@ -150,9 +204,10 @@ class ParameterHomotopy:
         return ParameterHomotopy(self.system, p, q)
 
 
-def parameter_homotopy(F: ParametricSystem, start_parameters=None, target_parameters=None,
-                       generic_parameters=None, seed: Optional[int] = None) -> ParameterHomotopy:
-    """src/solve.jl:233-260: missing parameters default to one generic complex vector."""
+def parameter_homotopy(F, start_parameters=None, target_parameters=None,
+                       generic_parameters=None, seed: Optional[int] = None):
+    """src/solve.jl:233-260: missing parameters default to one generic complex vector. F: a
+    ParametricSystem or an ``slp.Program`` with parameters."""
     if generic_parameters is None:
         rng = np.random.Generator(np.random.PCG64(seed))
         generic_parameters = (rng.standard_normal(F.nparams) + 1j * rng.standard_normal(F.nparams)) / np.sqrt(2)
@@ -191,6 +246,20 @@ def solve(F: ParametricSystem, starts, start_parameters, target_parameters, trac
     transform_result = transform_result or (lambda r, q: (r, q))
     transform_parameters = transform_parameters or (lambda q: q)
     targets = list(target_parameters)
+    from .slp import Program
+
+    if isinstance(F, Program):
+        # one compiled program, retargeted per target parameters (two small device arrays)
+        T = EndgameTracker(ParameterHomotopy(F, start_parameters, transform_parameters(targets[0])), to, eo)
+        out = []
+        for q in targets:
+            T.set_homotopy(ParameterHomotopy(F, start_parameters, transform_parameters(q)))
+            r = transform_result(Result(T.track_batch(S), start_system=None), q)
+            if flatten:
+                out.extend(r)
+            else:
+                out.append(r)
+        return out
     Hs = [ParameterHomotopy(F, start_parameters, transform_parameters(q)) for q in targets]
     B = BatchTracker(Hs, to, eo, npaths=[S.shape[0]] * len(Hs))
     results = B.solve(starts=np.tile(S.reshape(-1), len(Hs)), start_system=None)

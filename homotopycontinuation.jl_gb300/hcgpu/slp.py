@@ -14,6 +14,13 @@ src/model_kit/compiled_system_homotopy.jl:39-57).
     F = Program([x[0] * x[1] - 1, (x[0] + x[1]) ** 2 - x[2], x[2] / (x[0] - 3) + 2], degrees=[2, 2, 2])
     H = slp_homotopy(F, gamma)              # γ t G + (1 - t) F, G the total-degree start system
     T = EndgameTracker(H); T.track_arrays(total_degree_start_solutions(H.degrees))
+
+A program may also have parameters (``variables_and_parameters``), entering it in any way the
+ops allow; ``slp_parameter_homotopy(F, p, q)`` is then the reference's ParameterHomotopy
+H(x, t) = F(x; t p + (1 - t) q) (src/homotopies/parameter_homotopy.jl:3-44), tracked from
+solutions of F(x; p) at t = 1 to t = 0 (``hc_set_slp_parameter_homotopy``); ``F.fixed(p)`` is
+F(·; p) as a parameter-free program (``fix_parameters``), e.g. to find start solutions by a
+total-degree solve.
 """
 from __future__ import annotations
 
@@ -38,10 +45,12 @@ INSTR_DTYPE = np.dtype([("input", np.int32, 4), ("op", np.int32), ("output", np.
 
 
 class _Tape:
-    """Records instructions; nodes are ('c', k) constants, ('x', j) variables, ('t', k) outputs."""
+    """Records instructions; nodes are ('c', k) constants, ('x', j) variables, ('p', k)
+    parameters, ('t', k) outputs."""
 
-    def __init__(self, n):
+    def __init__(self, n, nparams=0):
         self.n = n
+        self.np = nparams
         self.consts: list = []
         self.cindex: dict = {}
         self.instr: list = []  # (op name, input nodes, exponent or None)
@@ -123,6 +132,13 @@ def variables(n: int):
     return [Expr(tape, ("x", j)) for j in range(n)]
 
 
+def variables_and_parameters(n: int, m: int):
+    """n tracing variables and m parameters of a new program (ModelKit's
+    ``System(f, variables, parameters)``): returns (x, p)."""
+    tape = _Tape(n, m)
+    return [Expr(tape, ("x", j)) for j in range(n)], [Expr(tape, ("p", k)) for k in range(m)]
+
+
 def op(name: str, *args: Expr, p: Optional[int] = None) -> Expr:
     """Record any ModelKit op by name, e.g. op("MULADD", a, b, c) = a*b + c, op("SQRT", a),
     op("POW_INT", a, p=-2)."""
@@ -137,10 +153,11 @@ def op(name: str, *args: Expr, p: Optional[int] = None) -> Expr:
 @dataclass
 class Program:
     """A square system F: C^n → C^n as a straight-line program, with the degrees of its
-    equations (the total-degree start system G_i = s_i (x_i^{D_i} - 1) uses them)."""
+    equations (the total-degree start system G_i = s_i (x_i^{D_i} - 1) uses them; without
+    parameters they default to the degrees ``degree_bounds`` finds)."""
 
     outputs: Sequence
-    degrees: Sequence[int]
+    degrees: Optional[Sequence[int]] = None
     scaling: Optional[Sequence[float]] = None
 
     def __post_init__(self):
@@ -149,24 +166,40 @@ class Program:
         if tape is None:
             raise ValueError("at least one output must depend on the variables")
         self.n = tape.n
-        if len(outs) != self.n or len(self.degrees) != self.n:
-            raise ValueError("a square system: n outputs and n degrees")
+        self.nparams = tape.np
         self._tape = tape
         self.outputs = [o if isinstance(o, Expr) else Expr(tape, tape.const(o)) for o in outs]
+        if self.degrees is None:
+            if self.nparams == 0:
+                self.degrees = self.degree_bounds()
+            else:  # no start system: the bounds where they exist (not used by the tracker)
+                try:
+                    self.degrees = self.degree_bounds()
+                except ValueError:
+                    self.degrees = [1] * self.n
+        if len(outs) != self.n or len(self.degrees) != self.n:
+            raise ValueError("a square system: n outputs and n degrees")
         if self.scaling is None:
             self.scaling = [1.0] * self.n
 
+    @property
+    def poff(self) -> int:
+        """Tape slot of the first parameter (after the constants and the variables)."""
+        return len(self._tape.consts) + self.n
+
     def arrays(self):
         """(instructions, constants re/im, variables_offset, tape_size, outputs) with constants at
-        slots [0, nconst), variables next, instruction outputs after them."""
+        slots [0, nconst), variables next, then the parameters (``poff``), instruction outputs
+        after them."""
         t = self._tape
         nc = len(t.consts)
         voff = nc
-        base = voff + self.n
+        poff = voff + self.n
+        base = poff + self.nparams
 
         def slot(node):
             kind, k = node
-            return k if kind == "c" else (voff + k if kind == "x" else base + k)
+            return {"c": k, "x": voff + k, "p": poff + k}.get(kind, base + k)
 
         ins = np.zeros(len(t.instr), dtype=INSTR_DTYPE)
         for k, (name, inputs, p) in enumerate(t.instr):
@@ -180,19 +213,92 @@ class Program:
         outs = np.array([slot(o.node) for o in self.outputs], dtype=np.int32)
         return ins, consts, voff, base + len(t.instr), outs
 
-    def evaluate(self, x):
-        """F(x) with numpy complex arithmetic (the ops' semantics; for tests)."""
+    def evaluate(self, x, p=None):
+        """F(x) (F(x; p) with parameters) with numpy complex arithmetic (the ops' semantics; for
+        tests)."""
         t = self._tape
         vals = {}
+        if self.nparams and p is None:
+            raise ValueError(f"the program has {self.nparams} parameters")
 
         def v(node):
             kind, k = node
-            return t.consts[k] if kind == "c" else (complex(x[k]) if kind == "x" else vals[k])
+            if kind == "c":
+                return t.consts[k]
+            if kind == "x":
+                return complex(x[k])
+            if kind == "p":
+                return complex(p[k])
+            return vals[k]
 
-        for k, (name, inputs, p) in enumerate(t.instr):
+        for k, (name, inputs, pw) in enumerate(t.instr):
             a = [v(i) for i in inputs]
-            vals[k] = _apply(name, a, p)
+            vals[k] = _apply(name, a, pw)
         return np.array([v(o.node) for o in self.outputs])
+
+
+    def degree_bounds(self):
+        """Upper bounds of the equations' degrees in x, by propagation through the ops (exact
+        for the sums, products and powers of polynomials); raises ValueError where an output
+        depends on the variables through a division, inverse or square root."""
+        t = self._tape
+        deg = {}
+
+        def d(node):
+            kind, k = node
+            return 1 if kind == "x" else (0 if kind in ("c", "p") else deg[k])
+
+        inf = float("inf")
+        for k, (name, inputs, p) in enumerate(t.instr):
+            a = [d(i) for i in inputs]
+            if name in ("ADD", "SUB", "ADD3", "ADD4", "NEG", "IDENTITY"):
+                deg[k] = max(a)
+            elif name in ("MUL", "MUL3", "MUL4"):
+                deg[k] = sum(a)
+            elif name == "SQR":
+                deg[k] = 2 * a[0]
+            elif name == "CB":
+                deg[k] = 3 * a[0]
+            elif name == "POW_INT":
+                deg[k] = p * a[0] if p >= 0 else (0 if a[0] == 0 else inf)
+            elif name in ("MULADD", "MULSUB", "SUBMUL"):
+                deg[k] = max(a[0] + a[1], a[2])
+            elif name in ("MULMULADD", "MULMULSUB"):
+                deg[k] = max(a[0] + a[1], a[2] + a[3])
+            else:  # DIV, INV, INVSQR, INV_NOT_ZERO, SQRT: polynomial only in constants/parameters
+                deg[k] = 0 if max(a) == 0 else inf
+        out = [d(o.node) for o in self.outputs]
+        if any(v == inf for v in out):
+            raise ValueError("an equation is not polynomial in the variables: pass its degrees")
+        return [max(int(v), 1) for v in out]
+
+    def fixed(self, p, degrees=None) -> "Program":
+        """F(·; p): the program with its parameters replaced by the constants p (fix_parameters,
+        src/systems/fixed_parameter_system.jl)."""
+        if not self.nparams:
+            raise ValueError("the program has no parameters")
+        p = [complex(v) for v in np.asarray(p, dtype=np.complex128).reshape(-1)]
+        if len(p) != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {len(p)}")
+        t = self._tape
+        x = variables(self.n)
+        tape = x[0].tape
+        vals = {}
+
+        def node(nd):
+            kind, k = nd
+            if kind == "c":
+                return tape.const(t.consts[k])
+            if kind == "x":
+                return ("x", k)
+            if kind == "p":
+                return tape.const(p[k])
+            return vals[k]
+
+        for k, (name, inputs, pw) in enumerate(t.instr):
+            vals[k] = tape.op(name, [node(i) for i in inputs], pw)
+        outs = [Expr(tape, node(o.node)) for o in self.outputs]
+        return Program(outs, degrees if degrees is not None else None, scaling=list(self.scaling))
 
 
 def _apply(name, a, p):
@@ -295,6 +401,42 @@ def slp_homotopy(F: Program, gamma) -> SLPHomotopy:
     return SLPHomotopy(F, complex(gamma))
 
 
+@dataclass
+class SLPParameterHomotopy:
+    """H(x, t) = F(x; t p + (1 - t) q) (src/homotopies/parameter_homotopy.jl:3-44) with F a
+    Program with parameters: p = start_parameters (t = 1), q = target_parameters (t = 0)."""
+
+    program: Program
+    start_parameters: np.ndarray
+    target_parameters: np.ndarray
+
+    def __post_init__(self):
+        m = self.program.nparams
+        if m == 0:
+            raise ValueError("the program has no parameters")
+        self.start_parameters = np.asarray(self.start_parameters, dtype=np.complex128).reshape(-1)
+        self.target_parameters = np.asarray(self.target_parameters, dtype=np.complex128).reshape(-1)
+        if self.start_parameters.shape[0] != m or self.target_parameters.shape[0] != m:
+            raise ValueError(f"expected {m} start and target parameters")
+
+    @property
+    def n(self):
+        return self.program.n
+
+    def parameters(self, p, q) -> "SLPParameterHomotopy":
+        """The same program with new (p, q) (parameters!, :56-62); on a tracker that already
+        has the program this changes two small device arrays and compiles nothing."""
+        return SLPParameterHomotopy(self.program, p, q)
+
+    def evaluate(self, x, t):
+        t = complex(t)
+        return self.program.evaluate(x, t * self.start_parameters + (1 - t) * self.target_parameters)
+
+
+def slp_parameter_homotopy(F: Program, start_parameters, target_parameters) -> SLPParameterHomotopy:
+    return SLPParameterHomotopy(F, start_parameters, target_parameters)
+
+
 class hc_slp(ct.Structure):
     _fields_ = [("n", ct.c_int32), ("ninstructions", ct.c_int32), ("instructions", ct.c_void_p),
                 ("nconstants", ct.c_int32), ("constants", ct.c_void_p), ("variables_offset", ct.c_int32),
@@ -315,15 +457,22 @@ def c_program(P: Program):
 
 
 def source(P: Program) -> str:
-    """The CUDA C that hc_set_slp compiles for P (no GPU needed)."""
+    """The CUDA C that hc_set_slp (hc_set_slp_parameter_homotopy for a program with
+    parameters) compiles for P (no GPU needed)."""
     from . import _lib
 
     L = _lib.load()
     s, deg, sc, keep = c_program(P)
     n = ct.c_int64()
-    _lib.check(L.hc_slp_source(ct.byref(s), _lib.ptr(deg), _lib.ptr(sc), None, 0, ct.byref(n)))
+
+    def call(out, cap):
+        if P.nparams:
+            return L.hc_slp_parameter_source(ct.byref(s), P.nparams, P.poff, out, cap, ct.byref(n))
+        return L.hc_slp_source(ct.byref(s), _lib.ptr(deg), _lib.ptr(sc), out, cap, ct.byref(n))
+
+    _lib.check(call(None, 0))
     buf = ct.create_string_buffer(n.value + 1)
-    _lib.check(L.hc_slp_source(ct.byref(s), _lib.ptr(deg), _lib.ptr(sc), buf, n.value + 1, ct.byref(n)))
+    _lib.check(call(buf, n.value + 1))
     return buf.value.decode()
 
 

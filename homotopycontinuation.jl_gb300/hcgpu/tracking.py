@@ -196,8 +196,22 @@ class _Handle:
         self.n = 0
 
     def set_homotopy(self, H):
-        from .slp import SLPHomotopy, c_program
+        from .slp import SLPHomotopy, SLPParameterHomotopy, c_program
 
+        if isinstance(H, SLPParameterHomotopy):  # F(x; t p + (1 - t) q), F a program
+            p = np.ascontiguousarray(H.start_parameters)
+            q = np.ascontiguousarray(H.target_parameters)
+            if getattr(self, "_param_program", None) is H.program:  # same program: new (p, q) only
+                _lib.check(self.L.hc_set_slp_parameters(self.h, _lib.ptr(p), _lib.ptr(q)), self.h)
+                return
+            s, deg, sc, keep = c_program(H.program)
+            self._keep = (s, deg, sc, keep)
+            _lib.check(self.L.hc_set_slp_parameter_homotopy(self.h, ct.byref(s), H.program.nparams, H.program.poff,
+                                                            _lib.ptr(p), _lib.ptr(q)), self.h)
+            self._param_program = H.program
+            self.n = H.n
+            return
+        self._param_program = None
         if isinstance(H, SLPHomotopy):  # F as a straight-line program (hc_set_slp)
             s, deg, sc, keep = c_program(H.program)
             self._keep = (s, deg, sc, keep)
@@ -519,9 +533,10 @@ def solve(F, starts=None, start_system: str = "total_degree", *, start_parameter
     GPU call replaces threaded_solve's per-path loop (src/solve.jl:628-709); the polyhedral start
     system tracks its toric stage and its coefficient homotopy as one launch each.
 
-    With ``start_parameters`` (F a parameters.ParametricSystem, ``starts`` its solutions at the
-    start parameters): the parameter homotopy to ``target_parameters``; a list of target
-    parameter vectors runs the many-parameter solver in one launch (src/solve.jl:747-880)."""
+    With ``start_parameters`` (F a parameters.ParametricSystem or an slp.Program with parameters,
+    ``starts`` its solutions at the start parameters): the parameter homotopy to
+    ``target_parameters``; a list of target parameter vectors runs the many-parameter solver
+    (src/solve.jl:747-880), in one launch for term tables."""
     if start_parameters is not None:
         from . import parameters
 

@@ -247,10 +247,12 @@ end
 
 # The reference's own program of F (src/model_kit/instruction_sequence.jl:133-254): its
 # instructions, constants and output slots with 0-based tape indices; OpType values are
-# hc_op's (include/hcgpu.h). F must have no parameters (fix them first).
-function program_arrays(F::HC.System)
+# hc_op's (include/hcgpu.h). Without `parameters = true`, F must have no parameters (fix them
+# first); with it, their slots are returned as `poff`, `np`.
+function program_arrays(F::HC.System; parameters::Bool = false)
     seq = HC.ModelKit.instruction_sequence(F)
-    isempty(seq.parameters_range) || throw(ArgumentError("fix the parameters of F before passing its program"))
+    parameters || isempty(seq.parameters_range) ||
+        throw(ArgumentError("fix the parameters of F before passing its program"))
     isempty(seq.constants_range) || first(seq.constants_range) == 1 ||
         throw(ArgumentError("unexpected tape layout: constants must come first"))
     ins = map(seq.instructions) do I
@@ -269,8 +271,10 @@ function program_arrays(F::HC.System)
     for (i, k) in seq.u_assignments
         outputs[i] = Int32(k - 1)
     end
+    np = length(seq.parameters_range)
     (; ins, consts, nconst = length(seq.constants), voff = Int32(first(seq.variables_range) - 1),
-       tape = Int32(seq.tape_space_needed), outputs, n)
+       tape = Int32(seq.tape_space_needed), outputs, n, np = Int32(np),
+       poff = Int32(np > 0 ? first(seq.parameters_range) - 1 : 0))
 end
 
 # a handle holding γ t G + (1 - t) F with F the reference's program (hc_set_slp); G is the
@@ -288,6 +292,38 @@ function program_handle(F::HC.System, D, s, γ, o::HCOptions)
     h[], A.n
 end
 
+# a handle holding the parameter homotopy F(x; t p + (1 - t) q) (hc_set_slp_parameter_homotopy)
+# with F the reference's program, parameters and all
+function parameter_program_handle(F::HC.System, p, q, o::HCOptions)
+    A = program_arrays(F; parameters = true)
+    A.np == length(p) == length(q) || throw(ArgumentError("expected $(A.np) start and target parameters"))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hc_create, libhcgpu), Cint, (Ref{HCOptions}, Ref{Ptr{Cvoid}}), Ref(o), h))
+    pp = ComplexF64.(p)
+    qq = ComplexF64.(q)
+    GC.@preserve A pp qq begin
+        P = HCSlp(A.n, length(A.ins), pointer(A.ins), A.nconst, pointer(A.consts), A.voff, A.tape, pointer(A.outputs))
+        check(ccall((:hc_set_slp_parameter_homotopy, libhcgpu), Cint,
+                    (Ptr{Cvoid}, Ref{HCSlp}, Cint, Int32, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                    h[], Ref(P), A.np, A.poff, pp, qq), h[])
+    end
+    h[], A.n
+end
+
+"""
+    parameters!(T::GPUTracker, p, q)
+
+New start and target parameters for a tracker of a `ParameterHomotopy` (`parameters!`,
+src/homotopies/parameter_homotopy.jl:56-62): no recompilation.
+"""
+function parameters!(T, p, q)
+    pp = ComplexF64.(p)
+    qq = ComplexF64.(q)
+    check(ccall((:hc_set_slp_parameters, libhcgpu), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                T.handle, pp, qq), T.handle)
+    T
+end
+
 """
     GPUTracker(eg::EndgameTracker; precision = 1, step_control = 0, program = nothing)
 
@@ -298,7 +334,8 @@ residuals and decisions. `step_control`: 0 = the reference's rule, 1 = the learn
 (load its network with `set_step_model!` first). `program = F` (the `System` `eg` tracks
 towards) passes F's own instruction sequence, unexpanded, through `hc_set_slp` instead of its
 expanded term table — as the reference evaluates it, which matters where expansion loses
-accuracy (e.g. `(x - 10)^6` near its root).
+accuracy (e.g. `(x - 10)^6` near its root). A `ParameterHomotopy` (parameters entering F in any
+way) always goes through its program (`hc_set_slp_parameter_homotopy`).
 """
 mutable struct GPUTracker <: HC.AbstractPathTracker
     handle::Ptr{Cvoid}
@@ -307,7 +344,9 @@ mutable struct GPUTracker <: HC.AbstractPathTracker
     function GPUTracker(eg::HC.EndgameTracker; precision = 1, step_control = 0, program = nothing)
         o = hc_options(eg.tracker.options, eg.options; precision = precision, step_control = step_control)
         H = eg.tracker.homotopy
-        if program === nothing
+        if H isa HC.ParameterHomotopy
+            h, n = parameter_program_handle(HC.ModelKit.System(H.F), H.p, H.q, o)
+        elseif program === nothing
             h, n = homotopy_handle(H, o)
         else
             H isa HC.StraightLineHomotopy || throw(ArgumentError("a straight-line homotopy is needed"))
@@ -452,7 +491,8 @@ solvers (polyhedral, parameter or subspace homotopies) are returned unchanged.
 function solver_startsolutions(args...; precision = 1, step_control = 0, compile = false, kwargs...)
     solver, starts = HC.solver_startsolutions(args...; compile = compile, kwargs...)
     eg = solver.trackers[1]
-    if eg isa HC.EndgameTracker && eg.tracker.homotopy isa HC.StraightLineHomotopy
+    if eg isa HC.EndgameTracker &&
+       (eg.tracker.homotopy isa HC.StraightLineHomotopy || eg.tracker.homotopy isa HC.ParameterHomotopy)
         gt = GPUTracker(eg; precision = precision, step_control = step_control)
         return HC.Solver(gt; seed = solver.seed, start_system = solver.start_system), starts
     end
@@ -462,16 +502,25 @@ end
 """
     solve(args...; precision = 1, step_control = 0, kwargs...)
 
-`solve` with the reference's arguments and keywords (src/solve.jl:447-526). Total-degree and
-start/target-system solves track on the GPU (`solver_startsolutions` above); the polyhedral
-start system (the reference's default for systems without variable groups) runs both of its
-tracking stages on the GPU (`gpu_polyhedral`); many-parameter, subspace and parameter
-homotopies go to the reference's own `solve`.
+`solve` with the reference's arguments and keywords (src/solve.jl:447-526). Total-degree,
+start/target-system and parameter-homotopy solves (`solve(F, starts; start_parameters,
+target_parameters)` with one target) track on the GPU (`solver_startsolutions` above); the
+polyhedral start system (the reference's default for systems without variable groups) runs
+both of its tracking stages on the GPU (`gpu_polyhedral`); many-parameter and subspace solves
+go to the reference's own `solve`.
 """
 function solve(args...; precision = 1, step_control = 0, seed = rand(UInt32), start_system = nothing,
                target_parameters = nothing, target_subspaces = nothing, start_subspace = nothing,
                show_progress::Bool = true, threading::Bool = true, catch_interrupt::Bool = true,
                stop_early_cb = HC.always_false, kwargs...)
+    one_target = target_parameters !== nothing && !isempty(target_parameters) && first(target_parameters) isa Number
+    if one_target && target_subspaces === nothing && start_subspace === nothing && length(args) == 2 &&
+       args[1] isa HC.System
+        solver, starts = solver_startsolutions(args...; precision = precision, step_control = step_control,
+                                               seed = seed, target_parameters = target_parameters, kwargs...)
+        return HC.solve(solver, collect(starts); stop_early_cb = stop_early_cb, show_progress = show_progress,
+                        threading = threading, catch_interrupt = catch_interrupt)
+    end
     if target_parameters !== nothing || target_subspaces !== nothing || start_subspace !== nothing ||
        !(length(args) == 1 && args[1] isa HC.System)
         return HC.solve(args...; seed = seed, target_parameters = target_parameters,

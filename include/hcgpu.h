@@ -165,6 +165,21 @@ int hc_set_slp(hc_handle* h, const hc_slp* F, const int32_t* degrees, const doub
  * bytes and a terminating 0 into out (may be NULL); *length receives the full length. */
 int hc_slp_source(const hc_slp* F, const int32_t* degrees, const double* scaling, char* out, int64_t capacity,
                   int64_t* length);
+/* Parameter homotopy H(x, t) = F(x; t p + (1 - t) q) (src/homotopies/parameter_homotopy.jl:3-44)
+ * of a program F(x; p) whose tape holds its nparameters parameters at slots
+ * [parameters_offset, +nparameters) (after the variables in ModelKit's tapes,
+ * src/model_kit/instruction_sequence.jl:1-27); p (start parameters) and q (target parameters)
+ * are nparameters complex values each. The parameters may enter F in any way the program's
+ * ops allow. Replaces the handle's homotopy; hc_track from start solutions of F(x; p) at t = 1
+ * to t = 0 then solves F(x; q). */
+int hc_set_slp_parameter_homotopy(hc_handle* h, const hc_slp* F, int nparameters, int32_t parameters_offset,
+                                  const double* start_parameters, const double* target_parameters);
+/* New (p, q) for the program of hc_set_slp_parameter_homotopy (parameters!, :56-62): no new
+ * compilation. */
+int hc_set_slp_parameters(hc_handle* h, const double* start_parameters, const double* target_parameters);
+/* The CUDA C that hc_set_slp_parameter_homotopy compiles for F. */
+int hc_slp_parameter_source(const hc_slp* F, int nparameters, int32_t parameters_offset, char* out,
+                            int64_t capacity, int64_t* length);
 
 /* Track npaths start solutions (host arrays, npaths×n complex interleaved).
  *   endgame = 1: EndgameTracker from t = t1_re to 0 (track(eg, x), src/endgame_tracker.jl:902-914),

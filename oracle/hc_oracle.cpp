@@ -214,6 +214,7 @@ enum SlpOp {
 };
 struct Slp {
   int n = 0, voff = 0, tape = 0, nconst = 0;
+  int np = 0, poff = 0;  // parameters at tape slots [poff, poff + np)
   std::vector<int> ins;  // 6 per instruction: input[0..3], op, output
   std::vector<C> consts;
   std::vector<int> outputs;
@@ -304,12 +305,14 @@ static int slp_arity(int op) {
   if (op >= SOP_ADD4) return 4;
   return 0;
 }
-// all tape values at x (arithmetic S)
+// all tape values at x (arithmetic S); pv: the parameters' values (np of them, may be null
+// without parameters)
 template <class S>
-static void slp_tape(const Slp& P, const S* x, std::vector<S>& t) {
+static void slp_tape(const Slp& P, const S* x, std::vector<S>& t, const C* pv = nullptr) {
   t.assign(P.tape, zero_like(x[0]));
   for (int k = 0; k < P.nconst; ++k) t[k] = promote(P.consts[k], x[0]);
   for (int j = 0; j < P.n; ++j) t[P.voff + j] = x[j];
+  for (int k = 0; k < P.np; ++k) t[P.poff + k] = promote(pv[k], x[0]);
   for (size_t q = 0; q + 5 < P.ins.size(); q += 6) {
     int op = P.ins[q + 4];
     if (op == SOP_STOP) break;
@@ -351,9 +354,9 @@ static C slp_tangent(int op, const C* v, C c, const C* d, int p) {
   return cx(0.0);
 }
 // F(x) and its Jacobian (column-major m×n), one forward-mode sweep per variable
-static void slp_eval_jac(const Slp& P, const C* x, C* u, C* U) {
+static void slp_eval_jac(const Slp& P, const C* x, C* u, C* U, const C* pv = nullptr) {
   std::vector<C> t, dt;
-  slp_tape(P, x, t);
+  slp_tape(P, x, t, pv);
   for (int i = 0; i < P.n; ++i) u[i] = t[P.outputs[i]];
   for (int j = 0; j < P.n; ++j) {
     dt.assign(P.tape, cx(0.0));
@@ -409,13 +412,20 @@ static void ser_pow(const C* a, int p, C* c, int K) {
   else
     for (int k = 0; k <= K; ++k) c[k] = r[k];
 }
-static void slp_taylor(const Slp& P, int K, const C* tx, int nx, C* dv) {
+// pv, dv_p: the parameters' values and their first-order coefficients (parameter homotopy:
+// p(t + s) = p(t) + s (p - q)); null without parameters
+static void slp_taylor(const Slp& P, int K, const C* tx, int nx, C* dv, const C* pv = nullptr,
+                       const C* dpv = nullptr) {
   const int L = K + 1, n = P.n;
   std::vector<C> t((size_t)P.tape * L, cx(0.0));
   auto at = [&](int slot) { return &t[(size_t)slot * L]; };
   for (int k = 0; k < P.nconst; ++k) at(k)[0] = P.consts[k];
   for (int j = 0; j < n; ++j)
     for (int k = 0; k < L; ++k) at(P.voff + j)[k] = k < nx ? tx[(size_t)k * n + j] : cx(0.0);
+  for (int k = 0; k < P.np; ++k) {
+    at(P.poff + k)[0] = pv[k];
+    if (L > 1) at(P.poff + k)[1] = dpv[k];
+  }
   std::vector<C> a(L), b(L), c(L), e(L);
   for (size_t q = 0; q + 5 < P.ins.size(); q += 6) {
     int op = P.ins[q + 4];
@@ -595,11 +605,39 @@ struct Homotopy {
   C gamma;
   int n, m;
   bool toric = false;
+  // parameter homotopy (src/homotopies/parameter_homotopy.jl:3-44): H(x, t) = F(x; t p + (1-t) q)
+  // with F.slp a program with parameters
+  bool param = false;
+  std::vector<C> pp, pq;
   std::vector<double> w;     // weights of the current path (F's term order)
   mutable System Ft;         // F with the coefficients u·t^w at t = tc_t
   mutable std::vector<double> tpow;
   mutable double tc_t = NaN;
 };
+
+// tp! (parameter_homotopy.jl:64-87): the parameters at t and their t-derivative p - q
+static void param_at(const Homotopy& H, C t, std::vector<C>& pv, std::vector<C>& dp) {
+  const size_t m = H.pp.size();
+  pv.resize(m);
+  dp.resize(m);
+  for (size_t k = 0; k < m; ++k) {
+    if (t.im == 0.0) {
+      const double s = t.re, r = 1.0 - t.re;
+      pv[k] = C{s * H.pp[k].re + r * H.pq[k].re, s * H.pp[k].im + r * H.pq[k].im};
+    } else {
+      pv[k] = t * H.pp[k] + (cx(1.0) - t) * H.pq[k];
+    }
+    dp[k] = H.pp[k] - H.pq[k];
+  }
+}
+template <class S>
+static void param_eval(const Homotopy& H, const S* x, C t, S* u) {
+  std::vector<C> pv, dp;
+  param_at(H, t, pv, dp);
+  std::vector<S> tape;
+  slp_tape(*H.F.slp, x, tape, pv.data());
+  for (int i = 0; i < H.m; ++i) u[i] = tape[H.F.slp->outputs[i]];
+}
 
 // coeffs! (toric_homotopy.jl:147-180) for real t ≥ 0
 static const System& toric_sys(const Homotopy& H, double t) {
@@ -618,6 +656,7 @@ static const System& toric_sys(const Homotopy& H, double t) {
 
 // :96-104
 static void H_eval(const Homotopy& H, const C* x, C t, C* u) {
+  if (H.param) return param_eval(H, x, t, u);  // evaluate!(u, H.F, x, H.pt) (:89-92)
   if (H.toric) {
     sys_eval(toric_sys(H, t.re), x, u);
     return;
@@ -630,6 +669,12 @@ static void H_eval(const Homotopy& H, const C* x, C t, C* u) {
 }
 // :81-94 (DD residual rounded to F64 on store)
 static void H_eval_dd(const Homotopy& H, const CDD* x, C t, C* u) {
+  if (H.param) {
+    std::vector<CDD> f(H.m);
+    param_eval(H, x, t, f.data());
+    for (int i = 0; i < H.m; ++i) u[i] = round_c(f[i]);
+    return;
+  }
   if (H.toric) {
     std::vector<CDD> f(H.m);
     sys_eval(toric_sys(H, t.re), x, f.data());
@@ -644,6 +689,11 @@ static void H_eval_dd(const Homotopy& H, const CDD* x, C t, C* u) {
 }
 // :106-124
 static void H_eval_jac(const Homotopy& H, const C* x, C t, C* u, C* U) {
+  if (H.param) {  // evaluate_and_jacobian!(u, U, H.F, x, H.pt) (:94-97)
+    std::vector<C> pv, dp;
+    param_at(H, t, pv, dp);
+    return slp_eval_jac(*H.F.slp, x, u, U, pv.data());
+  }
   if (H.toric) {
     sys_eval_jac(toric_sys(H, t.re), x, u, U);
     return;
@@ -659,6 +709,13 @@ static void H_eval_jac(const Homotopy& H, const C* x, C t, C* u, C* U) {
 // :130-137  taylor!(u, Val(1), H, x, t) = γ G(x) - F(x);
 // toric (toric_homotopy.jl:133-146, 255-257): F(x; ċ), ċ = w·c/t (t = 0: u where w == 1)
 static void H_taylor1(const Homotopy& H, const C* x, C t, C* u) {
+  if (H.param) {  // taylor!(u, Val(1), H.F, x, tp!(H, t)): order 1 of F(x; p(t + s))
+    std::vector<C> pv, dp, dv((size_t)2 * H.m);
+    param_at(H, t, pv, dp);
+    slp_taylor(*H.F.slp, 1, x, 1, dv.data(), pv.data(), dp.data());
+    for (int i = 0; i < H.m; ++i) u[i] = dv[(size_t)H.m + i];
+    return;
+  }
   if (H.toric) {
     const System& Fc = toric_sys(H, t.re);
     System Fd = Fc;
@@ -680,6 +737,13 @@ static void H_taylor1(const Homotopy& H, const C* x, C t, C* u) {
 // :138-154  taylor!(u, Val(K), H, tx, t), tx holds K vectors (orders 0..K-1)
 static void H_taylorK(const Homotopy& H, int K, const C* tx, C t, C* u) {
   int m = H.m;
+  if (H.param) {  // taylor!(u, Val(K), H.F, tx, tp!(H, t)) (:98-101): order K of F(x(s); p(t + s))
+    std::vector<C> pv, dp, dv((size_t)(K + 1) * m);
+    param_at(H, t, pv, dp);
+    slp_taylor(*H.F.slp, K, tx, K, dv.data(), pv.data(), dp.data());
+    for (int i = 0; i < m; ++i) u[i] = dv[(size_t)K * m + i];
+    return;
+  }
   if (H.toric) {
     // taylor_coeffs! (toric_homotopy.jl:199-253): c^(j) = u·tw_j, tw_0 = t^w,
     // tw_1 = w tw_0/t, tw_2 = (w-1)/2 tw_1/t, tw_3 = (w-2) tw_2/t/3; u_K = Σ_j [ε^(K-j)] F(x(ε); c^(j))
@@ -1856,6 +1920,7 @@ static thread_local const long* tl_trace_eg = nullptr;
 static int64_t g_trace_path = -1;  // 0-based path index to trace (-1: none)
 static Slp g_slp;  // program of F for hco_track (hco_set_slp)
 static bool g_slp_on = false;
+static std::vector<C> g_param_p, g_param_q;  // parameter homotopy of g_slp (hco_set_slp_parameters)
 static std::vector<double> g_trace;
 
 // :851-926
@@ -2501,6 +2566,11 @@ int hco_track(int n, int nG, const int32_t* G_eq, const int32_t* G_exps, const d
   if (g_slp_on) {
     if (g_slp.n != n) return 1;
     H.F.slp = &g_slp;
+    if (g_slp.np > 0) {
+      H.param = true;
+      H.pp = g_param_p;
+      H.pq = g_param_q;
+    }
   }
   H.gamma = C{gamma_re, gamma_im};
   TrackerOptions to;
@@ -2728,6 +2798,15 @@ int hco_homotopy_eval(int n, int nG, const int32_t* G_eq, const int32_t* G_exps,
   H.n = H.m = n;
   H.G = make_system(n, n, nG, G_eq, G_exps, G_coef);
   H.F = make_system(n, n, nF, F_eq, F_exps, F_coef);
+  if (g_slp_on) {
+    if (g_slp.n != n) return 1;
+    H.F.slp = &g_slp;
+    if (g_slp.np > 0) {
+      H.param = true;
+      H.pp = g_param_p;
+      H.pq = g_param_q;
+    }
+  }
   H.gamma = C{gamma_re, gamma_im};
   C t{t_re, t_im};
   int nx = (kind >= 4) ? kind - 2 : 1;
@@ -2776,6 +2855,19 @@ void hco_set_slp(int n, int ninstr, const int32_t* instr, int nconst, const doub
   for (int k = 0; k < nconst; ++k) g_slp.consts.push_back(C{consts[2 * k], consts[2 * k + 1]});
   g_slp.outputs.assign(outputs, outputs + n);
   g_slp_on = true;
+}
+
+// The program of hco_set_slp as F(x; p) with np parameters at tape slots [poff, poff + np),
+// tracked as the parameter homotopy F(x; t p + (1 - t) q); p, q: np complex values each.
+void hco_set_slp_parameters(int np, int poff, const double* p, const double* q) {
+  g_slp.np = np;
+  g_slp.poff = poff;
+  g_param_p.assign(np, cx(0.0));
+  g_param_q.assign(np, cx(0.0));
+  for (int k = 0; k < np; ++k) {
+    g_param_p[k] = C{p[2 * k], p[2 * k + 1]};
+    g_param_q[k] = C{q[2 * k], q[2 * k + 1]};
+  }
 }
 
 // Step trace of one path of the next hco_track call (path: 0-based index, -1 = off); the

@@ -203,12 +203,14 @@ def track_toric(F_terms, weights, starts, rows, t1, t0, omega=None, mu=None, opt
     return res, xs
 
 
-def set_slp(program=None):
+def set_slp(program=None, start_parameters=None, target_parameters=None):
     """Evaluate F as the straight-line program ``program`` (hcgpu.slp.Program) in the following
-    track() calls; None switches back to term tables."""
+    track() / homotopy_eval() calls; None switches back to term tables. A program with
+    parameters is tracked as the parameter homotopy F(x; t p + (1 - t) q)."""
     L = lib()
     L.hco_set_slp.argtypes = [ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int,
                               ct.c_void_p]
+    L.hco_set_slp_parameters.argtypes = [ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]
     if program is None:
         L.hco_set_slp(0, -1, None, 0, None, 0, 0, None)
         return
@@ -218,6 +220,11 @@ def set_slp(program=None):
     outs = np.ascontiguousarray(outs, dtype=np.int32)
     L.hco_set_slp(program.n, len(ins), _ptr(flat), len(consts) // 2 if len(program._tape.consts) else 0,
                   _ptr(consts), voff, tape, _ptr(outs))
+    if getattr(program, "nparams", 0):
+        p = _cplx(start_parameters)
+        q = _cplx(target_parameters)
+        assert p.shape[0] == q.shape[0] == program.nparams
+        L.hco_set_slp_parameters(program.nparams, program.poff, _ptr(p), _ptr(q))
 
 
 def track_slp(program, gamma, starts, **kw):
@@ -236,6 +243,29 @@ def track_slp(program, gamma, starts, **kw):
     set_slp(program)
     try:
         return track(G, F, gamma, starts, **kw)
+    finally:
+        set_slp(None)
+
+
+def _no_terms(n):
+    return (np.zeros(0, np.int32), np.zeros((0, n), np.int32), np.zeros(0, np.complex128))
+
+
+def track_slp_parameter(program, start_parameters, target_parameters, starts, **kw):
+    """track() of the parameter homotopy F(x; t p + (1 - t) q), F = program (with parameters),
+    from start solutions of F(x; p) at t = 1 to t = 0."""
+    set_slp(program, start_parameters, target_parameters)
+    try:
+        return track(_no_terms(program.n), _no_terms(program.n), 1.0 + 0j, starts, **kw)
+    finally:
+        set_slp(None)
+
+
+def slp_parameter_eval(program, start_parameters, target_parameters, kind, x, t):
+    """homotopy_eval() of the parameter homotopy of ``program`` (kinds as there)."""
+    set_slp(program, start_parameters, target_parameters)
+    try:
+        return homotopy_eval(_no_terms(program.n), _no_terms(program.n), 1.0 + 0j, kind, x, t)
     finally:
         set_slp(None)
 

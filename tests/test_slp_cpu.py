@@ -85,7 +85,7 @@ def test_program_validation():
     # a temporary slot may be written again (compacted tapes); a variable may not
     assert _raw(ok[:2] + [((1, 2), "ADD", 3)], 1, [1.0, 0.0], 1, 6, [4, 3], 2)[0] == 0
     rc, msg = _raw(ok[:2] + [((1, 2), "ADD", 2)], 1, [1.0, 0.0], 1, 6, [4, 5], 2)
-    assert rc == 1 and "constant or variable" in msg
+    assert rc == 1 and "a constant, variable or parameter" in msg
     rc, msg = _raw(ok, 1, [1.0, 0.0], 1, 6, [4, 7], 2)
     assert rc == 1 and "never written" in msg
     rc, msg = _raw([((1, 99), "POW_INT", 3)] + ok[1:], 1, [1.0, 0.0], 1, 6, [4, 5], 2)
