@@ -21,9 +21,9 @@ cudaError_t launch_track(const Launch& la, int blocks, int warps_per_cta, cudaSt
 cudaError_t occupancy(int precision, int warps_per_cta, size_t smem, int* blocks_per_sm);
 cudaError_t prepare_batch(int precision, size_t smem, int warps_per_cta, int* blocks_per_sm);
 int certify_layout(const DevProg& P, int* bytes_out);
-cudaError_t launch_certify(const DevProg& P, int64_t nsols, const double* d_in, hc_certificate* d_out,
-                           double* d_centers, double* d_enclosures, int real_coefficients, int num_sms,
-                           cudaStream_t stream);
+cudaError_t launch_certify(const DevProg& P, int64_t nitems, const int64_t* d_list, bool dw, const double* d_in,
+                           hc_certificate* d_out, double* d_centers, double* d_enclosures, int real_coefficients,
+                           int num_sms, cudaStream_t stream);
 cudaError_t launch_batch(const BatchLaunch& bl, int blocks, int warps_per_cta, size_t smem, cudaStream_t stream);
 }  // namespace hcd
 
@@ -1964,9 +1964,27 @@ int hc_certify(hc_handle* h, int64_t ncand, const double* cand, int real_coeffic
   static_assert(sizeof(hc_certificate) <= sizeof(hc_path_result), "certificates reuse the result buffer");
   hc_certificate* d_cert = (hc_certificate*)h->d_res;
   CK(cudaMemcpyAsync(h->d_starts, cand, nv * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
-  CK(launch_certify(h->dprog, ncand, (const double*)h->d_starts, d_cert, (double*)h->d_sol, (double*)h->d_last,
-                    real_coefficients ? 1 : 0, h->num_sms, h->stream));
+  CK(launch_certify(h->dprog, ncand, nullptr, false, (const double*)h->d_starts, d_cert, (double*)h->d_sol,
+                    (double*)h->d_last, real_coefficients ? 1 : 0, h->num_sms, h->stream));
   CK(cudaMemcpyAsync(out, d_cert, (size_t)ncand * sizeof(hc_certificate), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  // the candidates FP64 balls did not certify, again with double-word centres
+  std::vector<int64_t> again;
+  for (int64_t k = 0; k < ncand; ++k)
+    if (!out[k].certified) again.push_back(k);
+  if (!again.empty()) {
+    if (h->plist_cap < again.size()) {
+      cudaFree(h->d_plist);
+      h->d_plist = nullptr;
+      h->plist_cap = 0;
+      CK(cudaMalloc(&h->d_plist, again.size() * sizeof(int64_t)));
+      h->plist_cap = again.size();
+    }
+    CK(cudaMemcpyAsync(h->d_plist, again.data(), again.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    CK(launch_certify(h->dprog, (int64_t)again.size(), h->d_plist, true, (const double*)h->d_starts, d_cert,
+                      (double*)h->d_sol, (double*)h->d_last, real_coefficients ? 1 : 0, h->num_sms, h->stream));
+    CK(cudaMemcpyAsync(out, d_cert, (size_t)ncand * sizeof(hc_certificate), cudaMemcpyDeviceToHost, h->stream));
+  }
   CK(cudaMemcpyAsync(out_centers, h->d_sol, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(out_enclosures, h->d_last, nv * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));

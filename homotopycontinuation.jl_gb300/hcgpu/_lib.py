@@ -90,7 +90,7 @@ EXPORTS = [
 ]
 STEP_LOG_FIELDS = 36
 CERT_DTYPE = np.dtype([("certified", np.int32), ("realness", np.int32), ("radius", np.float64),
-                       ("enclosure", np.float64)])
+                       ("enclosure", np.float64), ("precision", np.int32), ("reserved", np.int32)])
 
 _lib = None
 

@@ -3,7 +3,8 @@
 Every candidate gets a Krawczyk certificate from ``hc_certify`` (csrc/hc_certify.cu): a polydisc
 B = B(center, radius) that provably contains exactly one solution, which lies in the smaller
 polydisc K = B(enclosure center, enclosure), and whether that solution is provably real or
-non-real. Distinctness is decided here from the certificates: two certified candidates name the
+non-real. Candidates that FP64 balls cannot certify are retried with double-word centres
+(``precision`` 106), as the reference retries with Arb balls. Distinctness is decided here from the certificates: two certified candidates name the
 same solution if one's K lies in the other's B (that B holds a single solution), and different
 solutions if their K's are disjoint; pairs where neither holds are counted as distinct and
 reported in ``nundecided_pairs``.
@@ -30,6 +31,7 @@ class SolutionCertificate:
     enclosure_center: np.ndarray
     enclosure: float
     index: int
+    precision: int = 53  # bits of the centres that decided (106: the double-word pass)
 
     def is_certified(self):
         return self.certified
@@ -138,7 +140,8 @@ def certify(F: System, solutions) -> CertificationResult:
     certs = [SolutionCertificate(solution_candidate=S[k].copy(), certified=bool(out["certified"][k]),
                                  real=bool(out["realness"][k] == 1), complex=bool(out["realness"][k] == 2),
                                  center=centers[k].copy(), radius=float(out["radius"][k]),
-                                 enclosure_center=encl[k].copy(), enclosure=float(out["enclosure"][k]), index=k)
+                                 enclosure_center=encl[k].copy(), enclosure=float(out["enclosure"][k]), index=k,
+                                 precision=int(out["precision"][k]))
              for k in range(len(S))]
     classes, undecided = _classes(certs)
     return CertificationResult(certs, classes, undecided)

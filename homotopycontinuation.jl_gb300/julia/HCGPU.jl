@@ -607,6 +607,8 @@ struct HCCertificate  # hc_certificate
     realness::Int32
     radius::Float64
     enclosure::Float64
+    precision::Int32  # 53, or 106 for the double-word pass
+    reserved::Int32
 end
 
 """

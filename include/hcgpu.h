@@ -386,11 +386,15 @@ int hc_track_batch(hc_handle* h, const double* starts, int endgame, hc_path_resu
  * certified = 1 if the polydisc B(center, radius) provably holds exactly one solution, which lies
  * in the polydisc B(enclosure center, enclosure); realness = 1 if that solution is provably real
  * (requires real_coefficients != 0, i.e. F has real coefficients), 2 if provably non-real, 0 if
- * undecided. center is the candidate after one Newton step. Ball arithmetic in FP64 with upward
- * rounded radii; one warp per candidate. */
+ * undecided. center is the candidate after Newton refinement. Ball arithmetic with upward rounded
+ * radii, one warp per candidate: first with FP64 centres (precision = 53), then, for the
+ * candidates that pass fails, with double-word centres (precision = 106; the reference's Arb step,
+ * src/certification.jl:1120-1200). */
 typedef struct hc_certificate {
   int32_t certified, realness;
   double radius, enclosure;
+  int32_t precision; /* bits of the centres of the pass that decided: 53 or 106 */
+  int32_t reserved;
 } hc_certificate;
 int hc_certify(hc_handle* h, int64_t ncandidates, const double* candidates, int real_coefficients,
                hc_certificate* out, double* out_centers, double* out_enclosure_centers);

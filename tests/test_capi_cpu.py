@@ -65,6 +65,20 @@ def test_instance_desc_layout_matches_header(tmp_path):
     assert onp == InstanceDesc.npaths.offset
 
 
+def test_certificate_layout_matches_header(tmp_path):
+    src = tmp_path / "cert.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "hcgpu.h"\n'
+        "int main(void){printf(\"%zu %zu %zu\\n\", sizeof(hc_certificate), offsetof(hc_certificate, enclosure),"
+        " offsetof(hc_certificate, precision));return 0;}\n")
+    exe = tmp_path / "cert"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    size, oe, op = map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split())
+    assert size == _lib.CERT_DTYPE.itemsize
+    assert oe == _lib.CERT_DTYPE.fields["enclosure"][1]
+    assert op == _lib.CERT_DTYPE.fields["precision"][1]
+
+
 def test_default_options_mirror_reference():
     o = _lib.default_options()
     # src/tracker.jl:45-62, :105-140 and src/endgame_tracker.jl:47-72
