@@ -53,24 +53,57 @@ __global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant_
     __syncthreads();
     T->init(la, wbase, tbase);
     __syncwarp();
-    while (true) {
+    auto take = [&](int64_t& kk) -> bool {  // the next path of the unit
       unsigned k = 0;
       if (lane == 0) k = atomicAdd(&s_next, 1u);
       k = __shfl_sync(FULL, k, 0);
-      const int64_t kk = (int64_t)U.lo + k;
-      if (kk >= U.hi) break;
-      if (T->cancelled()) {
-        if (lane == 0) {
-          hc_path_result R;
-          memset(&R, 0, sizeof(R));
-          R.path_number = kk + 1;
-          R.return_code = la->mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
-          la->res[kk] = R;
-        }
-        continue;
+      kk = (int64_t)U.lo + k;
+      return kk < U.hi;
+    };
+    auto cancel_result = [&](int64_t kk) {
+      if (lane == 0) {
+        hc_path_result R;
+        memset(&R, 0, sizeof(R));
+        R.path_number = kk + 1;
+        R.return_code = la->mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
+        la->res[kk] = R;
       }
-      T->run(kk);
-      ++npaths_done;
+    };
+    if (!bl.base.lockstep) {
+      int64_t kk;
+      while (take(kk)) {
+        if (T->cancelled()) {
+          cancel_result(kk);
+          continue;
+        }
+        T->run(kk);
+        ++npaths_done;
+      }
+    } else {
+      // lockstep within the unit (see track_kernel): one step per warp per round, then a barrier
+      bool active = false, done = false;
+      int64_t kk = 0;
+      while (true) {
+        if (!active && !done) {
+          if (!take(kk)) {
+            done = true;
+          } else if (T->cancelled()) {
+            cancel_result(kk);
+          } else {
+            T->begin(kk);
+            active = T->tracking();
+            if (!active) {
+              T->finish(kk);
+              ++npaths_done;
+            }
+          }
+        } else if (active && !T->step()) {
+          T->finish(kk);
+          active = false;
+          ++npaths_done;
+        }
+        if (__syncthreads_and(done && !active)) break;
+      }
     }
   }
   __syncwarp();

@@ -2585,27 +2585,52 @@ struct PathTracker {
   }
 
   // ---------------------------------------------------------------- one path
-  __device__ HC_NI void run(int64_t k) {
-    HC_PHASE(PH_RUN);
+  // One path in three parts, so that a kernel can also advance many paths one step at a time:
+  // begin (start solution, tracker/endgame init), step (one endgame or tracker step; false once
+  // the path stops), finish (result record and endpoint).
+  __device__ HC_NI void begin(int64_t k) {
     cur_path = k;
     if (LANE < n) {
       double2 s = a->starts[k * n + LANE];
       x[LANE] = C64(s.x, s.y);
     }
     __syncwarp();
+    if (a->mode == 1) {
+      eg_init(a->t1_re);
+    } else {
+      c64 t1 = C64(a->t1_re, a->t1_im), t0 = C64(a->t0_re, a->t0_im);
+      if (a->path_t1) t1 = C64(a->path_t1[k], 0.0);
+      if (a->path_t0) t0 = C64(a->path_t0[k], 0.0);
+      const double om_in = a->path_omega ? a->path_omega[k] : dNaN();
+      const double mu_in = a->path_mu ? a->path_mu[k] : dNaN();
+      if (toric) {
+        const double* wr = a->tor_w + (size_t)a->tor_row[k] * a->L.tor_n;
+        for (int j = LANE; j < a->L.tor_n; j += 32) tw[j] = wr[j];
+        tc_t = dNaN();
+        __syncwarp();
+      }
+      tracker_init(t1, t0, om_in, mu_in);
+    }
+  }
+  __device__ __forceinline__ bool tracking() const {
+    return a->mode == 1 ? ecode == EC_tracking : tcode == TC_tracking;
+  }
+  __device__ HC_NI bool step() {
+    if (a->mode == 1) {
+      eg_step();
+      if (cancelled()) ecode = EC_terminated_unknown;
+    } else {
+      tracker_step();
+      if (cancelled()) tcode = TC_terminated_unknown;
+    }
+    return tracking();
+  }
+  __device__ HC_NI void finish(int64_t k) {
     hc_path_result R;
     memset(&R, 0, sizeof(R));
     R.path_number = k + 1;
     c64 xs;
     if (a->mode == 1) {
-      eg_init(a->t1_re);
-      while (ecode == EC_tracking) {
-        eg_step();
-        if (cancelled()) {
-          ecode = EC_terminated_unknown;
-          break;
-        }
-      }
       double t;
       const c64* xv;
       if (ecode == EC_success) {
@@ -2638,25 +2663,6 @@ struct PathTracker {
         if (a->last) a->last[k * n + LANE] = make_double2(lastp[LANE].re, lastp[LANE].im);
       }
     } else {
-      c64 t1 = C64(a->t1_re, a->t1_im), t0 = C64(a->t0_re, a->t0_im);
-      if (a->path_t1) t1 = C64(a->path_t1[k], 0.0);
-      if (a->path_t0) t0 = C64(a->path_t0[k], 0.0);
-      const double om_in = a->path_omega ? a->path_omega[k] : dNaN();
-      const double mu_in = a->path_mu ? a->path_mu[k] : dNaN();
-      if (toric) {
-        const double* wr = a->tor_w + (size_t)a->tor_row[k] * a->L.tor_n;
-        for (int j = LANE; j < a->L.tor_n; j += 32) tw[j] = wr[j];
-        tc_t = dNaN();
-        __syncwarp();
-      }
-      tracker_init(t1, t0, om_in, mu_in);
-      while (tcode == TC_tracking) {
-        tracker_step();
-        if (cancelled()) {
-          tcode = TC_terminated_unknown;
-          break;
-        }
-      }
       c64 t = ss.t();
       R.return_code = tcode;
       R.t_re = t.re;
@@ -2684,6 +2690,13 @@ struct PathTracker {
     if (LANE < n) a->sol[k * n + LANE] = make_double2(xs.re, xs.im);
     if (LANE == 0) a->res[k] = R;
     __syncwarp();
+  }
+  __device__ HC_NI void run(int64_t k) {
+    HC_PHASE(PH_RUN);
+    begin(k);
+    while (tracking())
+      if (!step()) break;
+    finish(k);
   }
 };
 

@@ -58,24 +58,60 @@ __global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Laun
   __syncwarp();
   const int lane = threadIdx.x & 31;
   unsigned long long npaths_done = 0;
-  while (true) {
+  auto take = [&](int64_t& kk) -> bool {  // the next path of the queue; false when it is empty
     unsigned long long k = 0;
     if (lane == 0) k = atomicAdd(la.counter, 1ULL);
     k = __shfl_sync(FULL, k, 0);
-    if (k >= (unsigned long long)la.npaths) break;
-    const int64_t kk = la.path_list ? la.path_list[k] : (int64_t)k;
-    if (T->cancelled()) {
-      if (lane == 0) {
-        hc_path_result R;
-        memset(&R, 0, sizeof(R));
-        R.path_number = kk + 1;
-        R.return_code = la.mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
-        la.res[kk] = R;
-      }
-      continue;
+    if (k >= (unsigned long long)la.npaths) return false;
+    kk = la.path_list ? la.path_list[k] : (int64_t)k;
+    return true;
+  };
+  auto cancel_result = [&](int64_t kk) {
+    if (lane == 0) {
+      hc_path_result R;
+      memset(&R, 0, sizeof(R));
+      R.path_number = kk + 1;
+      R.return_code = la.mode == 1 ? EC_terminated_unknown : TC_terminated_unknown;
+      la.res[kk] = R;
     }
-    T->run(kk);
-    ++npaths_done;
+  };
+  if (!la.lockstep) {
+    int64_t kk;
+    while (take(kk)) {
+      if (T->cancelled()) {
+        cancel_result(kk);
+        continue;
+      }
+      T->run(kk);
+      ++npaths_done;
+    }
+  } else {
+    // lockstep: per round, each warp with a path takes one step of it (a warp without one first
+    // takes the next path of the queue and begins it); then the CTA waits for all its warps.
+    // Every warp reaches the barrier once per round and all leave together.
+    bool active = false, done = false;
+    int64_t kk = 0;
+    while (true) {
+      if (!active && !done) {
+        if (!take(kk)) {
+          done = true;
+        } else if (T->cancelled()) {
+          cancel_result(kk);
+        } else {
+          T->begin(kk);
+          active = T->tracking();
+          if (!active) {
+            T->finish(kk);
+            ++npaths_done;
+          }
+        }
+      } else if (active && !T->step()) {
+        T->finish(kk);
+        active = false;
+        ++npaths_done;
+      }
+      if (__syncthreads_and(done && !active)) break;
+    }
   }
   __syncwarp();
   if (lane == 0 && la.stats) add_stats(la.stats, T, npaths_done);

@@ -53,6 +53,8 @@ class Options(ct.Structure):
         ("step_control", ct.c_int32),
         ("warps_per_cta", ct.c_int32),
         ("ctas_per_sm", ct.c_int32),
+        ("lockstep", ct.c_int32),
+        ("reserved", ct.c_int32),
     ]
 
 

@@ -58,6 +58,7 @@ class TrackerOptions:
     step_model: Optional[object] = None  # learn.StepModel for "learned"; None: the shipped model
     warps_per_cta: int = 0
     ctas_per_sm: int = 0
+    lockstep: int = -1  # 1: a CTA's warps step together, 0: each on its own, -1: automatic
 
 
 @dataclass
@@ -91,7 +92,7 @@ def make_options(tracker_options: Optional[TrackerOptions] = None,
         raise ValueError(f"Unsupported `parameters` value {to.parameters}")
     o = _lib.default_options()
     for f in ("max_steps", "max_step_size", "max_initial_step_size", "min_step_size", "min_rel_step_size",
-              "terminate_cond", "warps_per_cta", "ctas_per_sm"):
+              "terminate_cond", "warps_per_cta", "ctas_per_sm", "lockstep"):
         setattr(o, f, getattr(to, f))
     o.extended_precision = int(to.extended_precision)
     for k, v in _PARAMETER_PRESETS[to.parameters].items():
@@ -263,7 +264,7 @@ class _Handle:
                   "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"] + [
         "clk_" + p for p in ("run", "step", "predictor", "predict", "newton", "eval_jac", "eval", "taylor", "lu",
                              "solve", "norm", "stepsize", "endgame", "mono", "val_rows", "jac_rows", "refine",
-                             "init", "cond", "dd")] + ["paths_retracked"]
+                             "init", "cond", "dd")] + ["paths_retracked", "lockstep"]
 
     def stats(self):
         out = np.zeros(len(self.STAT_NAMES))

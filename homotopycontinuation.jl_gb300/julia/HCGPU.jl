@@ -67,6 +67,8 @@ struct HCOptions  # hc_options
     step_control::Int32
     warps_per_cta::Int32
     ctas_per_sm::Int32
+    lockstep::Int32   # 1 / 0 / -1 = automatic (hc_options)
+    reserved::Int32
 end
 
 struct HCPathResult  # hc_path_result

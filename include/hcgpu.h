@@ -70,6 +70,12 @@ typedef struct hc_options {
   int32_t step_control;   /* enum hc_step_control */
   int32_t warps_per_cta;  /* 0 = as many as fit in shared memory (at most 8), balanced per precision */
   int32_t ctas_per_sm;    /* 0 = as many as fit */
+  /* scheduling of a CTA's warps: 1 = lockstep (every warp advances its path by one step, then
+   * the CTA waits for all, so the warps run the same code together and share the instruction
+   * cache), 0 = each warp on its own, -1 = automatic (lockstep in mixed precision with at
+   * least 8 warps per CTA). Results are identical either way. */
+  int32_t lockstep;
+  int32_t reserved;
 } hc_options;
 
 /* Per-path record. Mirrors PathResult (src/path_result.jl:76-98) for endgame tracking and

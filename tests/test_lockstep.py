@@ -1,0 +1,66 @@
+"""Lockstep scheduling of a CTA's warps (hc_options::lockstep): every warp advances its path by
+one step per round and the CTA waits for all of them, so the warps run the same code together.
+Each path still runs the same operations in the same order, so results must be identical bit
+for bit to the per-warp schedule, for single launches and for batches, in both precisions, and
+the automatic choice must take lockstep exactly for mixed precision with 8 warps per CTA."""
+import numpy as np
+import pytest
+
+import hcgpu as hc
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["return_code", "t_re", "accuracy", "residual", "cond", "winding_number", "singular", "accepted_steps",
+          "rejected_steps", "steps_eg", "path_number"]
+
+
+def _same(ra, xa, rb, xb):
+    for f in FIELDS:
+        a, b = ra[f], rb[f]
+        assert np.array_equal(a, b, equal_nan=np.issubdtype(a.dtype, np.floating)), f
+    assert np.array_equal(xa, xb)
+
+
+@pytest.mark.parametrize("precision,step_control", [("mixed", "learned"), ("mixed", "plain"), ("fp64", "plain")])
+def test_lockstep_equals_per_warp_schedule(precision, step_control):
+    F, g = hc.dense_random_system(7, 3, seed=2)  # 2,187 paths; 8 warps per CTA fit in both layouts
+    H = hc.total_degree_homotopy(F, g)
+    S = hc.total_degree_start_solutions(H.degrees)
+    out = {}
+    for mode in (0, 1, -1):
+        to = hc.TrackerOptions(precision=precision, step_control=step_control, warps_per_cta=8, lockstep=mode)
+        T = hc.EndgameTracker(H, to)
+        r, x, _, _ = T.track_arrays(S)
+        out[mode] = (r, x, T.stats())
+    _same(out[0][0], out[0][1], out[1][0], out[1][1])
+    _same(out[0][0], out[0][1], out[-1][0], out[-1][1])
+    assert out[0][2]["lockstep"] == 0 and out[1][2]["lockstep"] == 1
+    assert out[-1][2]["lockstep"] == (1 if precision == "mixed" else 0)
+    # the plain tracker (no endgame) through the same kernel
+    r0, x0 = [], []
+    for mode in (0, 1):
+        T = hc.Tracker(H, hc.TrackerOptions(precision=precision, warps_per_cta=8, lockstep=mode))
+        r, x, _, _ = T.track_arrays(S[:512], t1=1.0, t0=0.1)
+        r0.append(r)
+        x0.append(x)
+    for f in ("return_code", "accepted_steps", "rejected_steps", "t_re"):
+        assert np.array_equal(r0[0][f], r0[1][f]), f
+    assert np.array_equal(x0[0], x0[1])
+
+
+def test_lockstep_in_batches():
+    inst = [(F, g) for F, g in hc.uneven_instances(40, 17) if F.n <= 7]
+    Hs = [hc.total_degree_homotopy(F, g) for F, g in inst]
+    res = []
+    for mode in (0, 1):
+        B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed", step_control="learned", lockstep=mode))
+        r, x = B.track_arrays()
+        res.append((r, x, B.stats()))
+    _same(res[0][0], res[0][1], res[1][0], res[1][1])
+    assert res[0][2]["lockstep"] == 0 and res[1][2]["lockstep"] == 1
+
+
+def test_lockstep_option_is_validated():
+    F, g = hc.dense_random_system(3, 2, seed=1)
+    with pytest.raises(hc._lib.HCError):
+        hc.EndgameTracker(hc.total_degree_homotopy(F, g), hc.TrackerOptions(lockstep=2))
