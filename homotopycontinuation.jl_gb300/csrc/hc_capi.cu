@@ -994,17 +994,20 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
 // launches use 4 rather than 5..7 (one CTA per SM; with 5..7 warps some of the SM's four
 // schedulers run two warps and the others one, and the FP32-phase-heavy mixed tracker lost
 // 5% at 5 warps against 4 on 10 dense cubics, while the FP64 tracker gained 10%).
-// Lockstep scheduling of a CTA's warps. Measured on 10 dense cubics (59,049 paths, one GB300):
-// with 8 warps per CTA in mixed precision, lockstep tracked 43.7k paths/s against 34.5k (learned
-// steps) and 25.6k against 21.2k (plain) — the warps share the instruction cache when they run
-// the same code — while with 4 or 5 warps it lost about 10% to the per-round waits.
+// Lockstep scheduling of a CTA's warps. Measured on one GB300 with 8 warps per CTA: 10 dense
+// cubics in mixed precision 43.7k paths/s against 34.5k (learned steps) and 25.6k against
+// 21.2k (plain); 8 sparse quartics +42..45% in either precision; 7 dense cubics in FP64 +24% —
+// the warps share the instruction cache when they run the same code. With 4 to 6 warps it
+// lost 6..10% to the per-round waits.
 static int lockstep_for(const hc_options& O, int wpc) {
   if (O.lockstep >= 0) return O.lockstep;
-  return O.precision == HC_PREC_MIXED && wpc >= 8 ? 1 : 0;
+  return wpc >= 8 ? 1 : 0;
 }
 
+// Mixed precision: 5 warps per CTA (two sub-partitions with two warps, two with one) measured
+// 5% below 4 on 10 dense cubics; 6 warps measured 16% above 4 on 11 dense cubics.
 static int balanced_warps(int wpc, int precision) {
-  if (precision == HC_PREC_MIXED && wpc > 4 && wpc < 8) return 4;
+  if (precision == HC_PREC_MIXED && wpc == 5) return 4;
   return wpc;
 }
 

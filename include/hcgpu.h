@@ -72,8 +72,8 @@ typedef struct hc_options {
   int32_t ctas_per_sm;    /* 0 = as many as fit */
   /* scheduling of a CTA's warps: 1 = lockstep (every warp advances its path by one step, then
    * the CTA waits for all, so the warps run the same code together and share the instruction
-   * cache), 0 = each warp on its own, -1 = automatic (lockstep in mixed precision with at
-   * least 8 warps per CTA). Results are identical either way. */
+   * cache), 0 = each warp on its own, -1 = automatic (lockstep with 8 warps per CTA).
+   * Results are identical either way. */
   int32_t lockstep;
   int32_t reserved;
 } hc_options;

@@ -2,7 +2,7 @@
 one step per round and the CTA waits for all of them, so the warps run the same code together.
 Each path still runs the same operations in the same order, so results must be identical bit
 for bit to the per-warp schedule, for single launches and for batches, in both precisions, and
-the automatic choice must take lockstep exactly for mixed precision with 8 warps per CTA."""
+the automatic choice must take lockstep with 8 warps per CTA."""
 import numpy as np
 import pytest
 
@@ -35,7 +35,7 @@ def test_lockstep_equals_per_warp_schedule(precision, step_control):
     _same(out[0][0], out[0][1], out[1][0], out[1][1])
     _same(out[0][0], out[0][1], out[-1][0], out[-1][1])
     assert out[0][2]["lockstep"] == 0 and out[1][2]["lockstep"] == 1
-    assert out[-1][2]["lockstep"] == (1 if precision == "mixed" else 0)
+    assert out[-1][2]["lockstep"] == 1  # automatic: 8 warps per CTA
     # the plain tracker (no endgame) through the same kernel
     r0, x0 = [], []
     for mode in (0, 1):
