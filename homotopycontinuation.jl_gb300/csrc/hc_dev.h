@@ -125,7 +125,8 @@ struct Launch {
   char* cold;  // per-warp global scratch of L.cold bytes (warp w of CTA b at (b·warps + w)·L.cold)
   // parameter homotopy of a straight-line program: p (start parameters) then q (target)
   const double2* slp_pq;
-  int lockstep;  // the CTA's warps advance their paths one step per round (hc_options::lockstep)
+  int lockstep;  // 1: the CTA's warps advance their paths one step per round; 2: the same per
+                 // sub-partition pair (hc_options::lockstep)
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant_
       }
     } else {
       // lockstep within the unit (see track_kernel): one step per warp per round, then a barrier
+      // of the CTA or of the warps sharing a sub-partition; the unit closes at the barrier above
       bool active = false, done = false;
       int64_t kk = 0;
       while (true) {
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant_
           active = false;
           ++npaths_done;
         }
-        if (__syncthreads_and(done && !active)) break;
+        if (lockstep_round(bl.base.lockstep, done && !active)) break;
       }
     }
   }

@@ -72,8 +72,10 @@ typedef struct hc_options {
   int32_t ctas_per_sm;    /* 0 = as many as fit */
   /* scheduling of a CTA's warps: 1 = lockstep (every warp advances its path by one step, then
    * the CTA waits for all, so the warps run the same code together and share the instruction
-   * cache), 0 = each warp on its own, -1 = automatic (lockstep with 8 warps per CTA).
-   * Results are identical either way. */
+   * cache), 2 = lockstep of the warps that share an SM sub-partition (warps w, w + 4), 0 = each
+   * warp on its own, -1 = automatic (batches: 1 with 8 warps per CTA; single homotopies: 2 in
+   * mixed precision with at least 6 warps per CTA, 1 in FP64 with 8). Results are identical in
+   * every mode. */
   int32_t lockstep;
   int32_t reserved;
 } hc_options;
