@@ -685,7 +685,7 @@ static const char* invalid_knob(const hc_options* o) {
   if (o->precision != HC_PREC_FP64 && o->precision != HC_PREC_MIXED) return "unknown precision";
   if (o->step_control != HC_STEP_PLAIN && o->step_control != HC_STEP_LEARNED && o->step_control != HC_STEP_EXPLORE)
     return "unknown step control";
-  if (o->lockstep < -1 || o->lockstep > 2) return "lockstep must be -1, 0, 1 or 2";
+  if (o->lockstep < -1 || o->lockstep > 3) return "lockstep must be -1, 0, 1, 2 or 3";
   return nullptr;
 }
 
@@ -994,18 +994,20 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
 // launches use 4 rather than 5..7 (one CTA per SM; with 5..7 warps some of the SM's four
 // schedulers run two warps and the others one, and the FP32-phase-heavy mixed tracker lost
 // 5% at 5 warps against 4 on 10 dense cubics, while the FP64 tracker gained 10%).
-// Lockstep scheduling of a CTA's warps. Measured on one GB300 (paths/s, per-warp → CTA-wide
-// lockstep → lockstep of the warps sharing a sub-partition): 10 dense cubics, mixed + learned,
-// 8 warps 34.5k → 43.9k → 45.2k, mixed + plain 21.2k → 25.8k → 27.9k; 11 dense cubics, mixed +
-// learned, 6 warps 25.9k → 24.3k → 27.8k; 8 sparse quartics, FP64 + learned, 8 warps 16.1k →
-// 23.2k → 19.5k; 7 dense cubics, FP64, 8 warps 22.8k → 28.4k; batch of 2,000 uneven instances
-// (a work unit's warps track one system), mixed + learned 61.6k → 90.8k → 75.2k, FP64 + plain
-// 25.7k → 31.8k (CTA-wide). The warps share the instruction cache when they run the same code;
-// with 4 or 5 warps the waits cost more than that gains.
+// Lockstep scheduling of a CTA's warps. Measured on one GB300 (paths/s; per-warp, then lockstep
+// of the CTA (1), of the warps of a sub-partition (2), of two sub-partitions (3)):
+//   10 dense cubics, mixed + learned, 8 warps   34.5k | 44.0k  44.5k  47.5k
+//   10 dense cubics, mixed + plain, 8 warps     21.2k | 25.6k  27.6k  28.7k
+//   11 dense cubics, mixed + learned, 6 warps   25.9k | 24.4k  27.8k  26.2k
+//   8 sparse quartics, FP64 + learned, 8 warps  16.1k | 23.2k  19.5k  22.2k
+//   7 dense cubics, FP64 + plain, 8 warps       22.8k | 28.4k
+//   2,000 uneven instances (batch), mixed + learned, 8 warps  61.6k | 89.2k  73.9k  85.6k
+// The warps share the instruction cache when they run the same code; with 4 or 5 warps the
+// waits cost more than that gains.
 static int lockstep_for(const hc_options& O, int wpc, bool batch = false) {
   if (O.lockstep >= 0) return O.lockstep;
   if (batch) return wpc >= 8 ? 1 : 0;
-  if (O.precision == HC_PREC_MIXED) return wpc >= 6 ? 2 : 0;
+  if (O.precision == HC_PREC_MIXED) return wpc >= 8 ? 3 : (wpc >= 6 ? 2 : 0);
   return wpc >= 8 ? 1 : 0;
 }
 
@@ -2057,7 +2059,8 @@ int hc_last_stats(hc_handle* h, double* out, int nout) {
   // monomial offset; [17] learned step proposals made, [18] of them rejected by Newton;
   // [19 ..] cycle counters of the tracker phases (HcPhase order; profiling builds only);
   // [19 + HC_NPHASE] paths re-tracked with plain step control by the jump check;
-  // [20 + HC_NPHASE] lockstep mode of the last launch (0 per warp, 1 CTA, 2 sub-partition pairs)
+  // [20 + HC_NPHASE] lockstep mode of the last launch (0 per warp, 1 CTA, 2 sub-partition, 3 two
+  // sub-partitions)
   double all[21 + HC_NPHASE];
   for (int i = 0; i < 9; ++i) all[i] = h->stats[i];
   all[9] = h->prog.M;
@@ -2144,8 +2147,8 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
     return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: learned step control needs a handle (hc_set_step_model)");
   if (opts->step_control != HC_STEP_PLAIN && opts->step_control != HC_STEP_EXPLORE)
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: unknown step control");
-  if (opts->lockstep < -1 || opts->lockstep > 2)
-    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: lockstep must be -1, 0, 1 or 2");
+  if (opts->lockstep < -1 || opts->lockstep > 3)
+    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: lockstep must be -1, 0, 1, 2 or 3");
   {
     // The compiled tables are copied from a host buffer that lives only for this call; a
     // copy recorded into a graph would read it after it is freed. Checked before any other

@@ -126,7 +126,7 @@ struct Launch {
   // parameter homotopy of a straight-line program: p (start parameters) then q (target)
   const double2* slp_pq;
   int lockstep;  // 1: the CTA's warps advance their paths one step per round; 2: the same per
-                 // sub-partition pair (hc_options::lockstep)
+                 // sub-partition; 3: per two sub-partitions (hc_options::lockstep)
 };
 
 // A batch of independent homotopies tracked in one launch (hc_set_batch / hc_track_batch).

@@ -16,19 +16,29 @@ __device__ __forceinline__ void stage(char* dst, const void* src, int bytes) {
   for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) d[i] = __ldg(s + i);
 }
 
-// End of a lockstep round (hc_options::lockstep): mode 1 waits for the whole CTA, mode 2 for the
-// warps that share this warp's SM sub-partition (warps w, w + 4, ...: named barrier 1 + w % 4 for
-// 32 threads per member). Every participating warp calls it once per round; returns true when
-// `done` holds in all of them, so they also leave the loop together.
+// End of a lockstep round (hc_options::lockstep): mode 1 waits for the whole CTA; mode 2 for the
+// warps that share this warp's SM sub-partition (warps w, w + 4, ...: named barrier 1 + w % 4);
+// mode 3 for the warps of sub-partitions {0, 1} or {2, 3} (named barrier 5 or 6). Named barriers
+// count 32 threads per member warp. Every participating warp calls it once per round; returns
+// true when `done` holds in all of them, so they also leave the loop together.
 __device__ __forceinline__ bool lockstep_round(int mode, bool done) {
-  if (mode != 2) return __syncthreads_and(done) != 0;
-  const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5, sub = wib & 3;
-  const int members = (nw - sub + 3) >> 2;
+  if (mode != 2 && mode != 3) return __syncthreads_and(done) != 0;
+  const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int id, members;
+  if (mode == 2) {
+    const int sub = wib & 3;
+    id = 1 + sub;
+    members = (nw - sub + 3) >> 2;
+  } else {
+    const int grp = (wib & 3) >> 1, rem = nw & 3;
+    id = 5 + grp;
+    members = 2 * (nw >> 2) + (grp == 0 ? (rem < 2 ? rem : 2) : (rem > 2 ? rem - 2 : 0));
+  }
   int all;
   asm volatile(
       "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.s32 %0, 1, 0, q;\n}"
       : "=r"(all)
-      : "r"(done ? 1 : 0), "r"(1 + sub), "r"(32 * members)
+      : "r"(done ? 1 : 0), "r"(id), "r"(32 * members)
       : "memory");
   return all != 0;
 }

@@ -58,7 +58,7 @@ class TrackerOptions:
     step_model: Optional[object] = None  # learn.StepModel for "learned"; None: the shipped model
     warps_per_cta: int = 0
     ctas_per_sm: int = 0
-    lockstep: int = -1  # 1: a CTA's warps step together, 2: warps sharing a sub-partition, 0: none, -1: auto
+    lockstep: int = -1  # lockstep of a CTA's warps: 1 all, 2 per sub-partition, 3 per two, 0 none, -1 auto
 
 
 @dataclass

@@ -72,10 +72,10 @@ typedef struct hc_options {
   int32_t ctas_per_sm;    /* 0 = as many as fit */
   /* scheduling of a CTA's warps: 1 = lockstep (every warp advances its path by one step, then
    * the CTA waits for all, so the warps run the same code together and share the instruction
-   * cache), 2 = lockstep of the warps that share an SM sub-partition (warps w, w + 4), 0 = each
-   * warp on its own, -1 = automatic (batches: 1 with 8 warps per CTA; single homotopies: 2 in
-   * mixed precision with at least 6 warps per CTA, 1 in FP64 with 8). Results are identical in
-   * every mode. */
+   * cache), 2 = lockstep of the warps that share an SM sub-partition (warps w, w + 4), 3 = of the
+   * warps of two sub-partitions, 0 = each warp on its own, -1 = automatic (batches: 1 with 8
+   * warps per CTA; single homotopies in mixed precision: 3 with 8 warps, 2 with 6 or 7; in
+   * FP64: 1 with 8). Results are identical in every mode. */
   int32_t lockstep;
   int32_t reserved;
 } hc_options;

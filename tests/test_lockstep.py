@@ -3,7 +3,7 @@ one step per round and the CTA (mode 1) or the warps sharing an SM sub-partition
 for each other, so the warps run the same code together. Each path still runs the same
 operations in the same order, so results must be identical bit for bit to the per-warp
 schedule, for single launches and for batches, in both precisions; the automatic choice takes
-mode 2 in mixed precision and mode 1 in FP64 with 8 warps per CTA, and mode 1 for batches."""
+mode 3 in mixed precision and mode 1 in FP64 with 8 warps per CTA, and mode 1 for batches."""
 import numpy as np
 import pytest
 
@@ -28,23 +28,23 @@ def test_lockstep_equals_per_warp_schedule(precision, step_control):
     H = hc.total_degree_homotopy(F, g)
     S = hc.total_degree_start_solutions(H.degrees)
     out = {}
-    for mode in (0, 1, 2, -1):
+    for mode in (0, 1, 2, 3, -1):
         to = hc.TrackerOptions(precision=precision, step_control=step_control, warps_per_cta=8, lockstep=mode)
         T = hc.EndgameTracker(H, to)
         r, x, _, _ = T.track_arrays(S)
         out[mode] = (r, x, T.stats())
-    for mode in (1, 2, -1):
+    for mode in (1, 2, 3, -1):
         _same(out[0][0], out[0][1], out[mode][0], out[mode][1])
-    assert [out[m][2]["lockstep"] for m in (0, 1, 2)] == [0, 1, 2]
-    assert out[-1][2]["lockstep"] == (2 if precision == "mixed" else 1)  # automatic, 8 warps per CTA
+    assert [out[m][2]["lockstep"] for m in (0, 1, 2, 3)] == [0, 1, 2, 3]
+    assert out[-1][2]["lockstep"] == (3 if precision == "mixed" else 1)  # automatic, 8 warps per CTA
     # the plain tracker (no endgame) through the same kernel
     r0, x0 = [], []
-    for mode in (0, 1, 2):
+    for mode in (0, 1, 2, 3):
         T = hc.Tracker(H, hc.TrackerOptions(precision=precision, warps_per_cta=8, lockstep=mode))
         r, x, _, _ = T.track_arrays(S[:512], t1=1.0, t0=0.1)
         r0.append(r)
         x0.append(x)
-    for m in (1, 2):
+    for m in (1, 2, 3):
         for f in ("return_code", "accepted_steps", "rejected_steps", "t_re"):
             assert np.array_equal(r0[0][f], r0[m][f]), f
         assert np.array_equal(x0[0], x0[m])
@@ -54,13 +54,13 @@ def test_lockstep_in_batches():
     inst = [(F, g) for F, g in hc.uneven_instances(40, 17) if F.n <= 7]
     Hs = [hc.total_degree_homotopy(F, g) for F, g in inst]
     res = []
-    for mode in (0, 1, 2):
+    for mode in (0, 1, 2, 3):
         B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed", step_control="learned", lockstep=mode))
         r, x = B.track_arrays()
         res.append((r, x, B.stats()))
-    for m in (1, 2):
+    for m in (1, 2, 3):
         _same(res[0][0], res[0][1], res[m][0], res[m][1])
-    assert [r[2]["lockstep"] for r in res] == [0, 1, 2]
+    assert [r[2]["lockstep"] for r in res] == [0, 1, 2, 3]
     B = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed", step_control="learned"))
     r, x = B.track_arrays()
     _same(res[0][0], res[0][1], r, x)
@@ -70,4 +70,4 @@ def test_lockstep_in_batches():
 def test_lockstep_option_is_validated():
     F, g = hc.dense_random_system(3, 2, seed=1)
     with pytest.raises(hc._lib.HCError):
-        hc.EndgameTracker(hc.total_degree_homotopy(F, g), hc.TrackerOptions(lockstep=3))
+        hc.EndgameTracker(hc.total_degree_homotopy(F, g), hc.TrackerOptions(lockstep=4))
