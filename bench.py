@@ -42,6 +42,12 @@ WORKLOADS = {
 }
 
 
+# hc_options::lockstep of the timed launch (hc_last_stats)
+LOCKSTEP_NAMES = {0: "none: each warp on its own", 1: "the CTA's warps step together",
+                  2: "the warps of each SM sub-partition step together",
+                  3: "the warps of each pair of SM sub-partitions step together"}
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -399,7 +405,8 @@ def main():
                        "precision": args.precision, "step_control": args.step_control,
                        "l2": "256 MiB buffer written between timed steps (inputs are smaller than L2)",
                        "parallelism": f"weak: one seeded instance per GPU x{world}",
-                       "warps_per_cta": stats["warps_per_block"], "ctas": stats["blocks"]},
+                       "warps_per_cta": stats["warps_per_block"], "ctas": stats["blocks"],
+                       "lockstep": LOCKSTEP_NAMES[int(stats["lockstep"])]},
             "e2e": e2e,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
@@ -575,6 +582,7 @@ def main_uneven(args, torch, hc, _lib, local):
             "config": {"workload": WORKLOADS["uneven"], "seed": args.seed, "instances": len(Hs),
                        "paths": B.total_paths, "precision": args.precision, "step_control": args.step_control,
                        "ctas": stats["blocks"], "warps_per_cta": stats["warps_per_block"],
+                       "lockstep": LOCKSTEP_NAMES[int(stats["lockstep"])],
                        "unit_paths": ({str(k): int(v) for k, v in unit_paths.items()} if unit_paths
                                       else "default: one path per warp of a CTA"),
                        "staging": ({str(k): v for k, v in staging.items()} if staging
