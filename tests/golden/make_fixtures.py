@@ -147,6 +147,13 @@ def main(ref):
                    r"@test_throws FiniteException\((\d+)\)", blk)
     out["parameter_solve"] = {"expect": {"nsolutions": int(n1.group(1)), "finite_exception_dim": int(fe.group(2))},
                               "underdetermined": to_param_system([fe.group(1)], ["x", "y"], ["a", "b"])}
+    # solve (DynamicPolynomials): nsolutions == 18 (test/solve_test.jl)
+    blk = sv[sv.index('@testset "solve (DynamicPolynomials)"'):]
+    d1 = re.search(r"f₁ = (.*)\n", blk).group(1).strip()
+    d2p = re.search(r"f₂ = (.*)\n", blk).group(1).strip()
+    out["dynamic_polynomials_18"] = {**to_system([d1, d2p], ["x", "y"]), "expect": {
+        "nsolutions": int(re.search(r"result = solve\(\[f₁, f₂\]\)\n\s*@test nsolutions\(result\) == (\d+)",
+                                    blk).group(1))}}
     # certification (test/certification_test.jl "Simple 1")
     ce = open(os.path.join(test, "certification_test.jl")).read()
     blk = ce[ce.index('@testset "Simple 1'):]

@@ -71,6 +71,19 @@ def test_cyclic7_total_degree(precision, step_control):
     assert_parity(ro, xo, rg, xg)
 
 
+@pytest.mark.parametrize("precision,step_control", MODES)
+def test_dynamic_polynomials_18(precision, step_control):
+    # test/solve_test.jl:338-344: 18 solutions of (x⁴ + y⁴ − 1)(x² + y² − 2) + x⁵y,
+    # x² + 2xy² − 2y² − 1/2 by total degree (every one of the 18 paths)
+    H = hc.total_degree_homotopy(system("dynamic_polynomials_18"), np.exp(2j * np.pi * 0.13))
+    S = hc.total_degree_start_solutions(H.degrees)
+    ro, xo, _, _ = oracle("dynamic_polynomials_18", H, S)
+    (rg, xg, _, _), _ = gpu_track(H, S, precision, step_control)
+    assert counts(rg)["nonsingular"] == KAT["dynamic_polynomials_18"]["expect"]["nsolutions"] == 18
+    assert counts(rg) == counts(ro)
+    assert_parity(ro, xo, rg, xg)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_wilkinson_12(precision):
     # test/endgame_test.jl:38-45: roots 1..12 (only_nonsingular endgame), tiny imaginary parts.

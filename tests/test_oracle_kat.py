@@ -70,6 +70,16 @@ def test_cyclic7():
     assert nonsingular(res) == KAT["cyclic7"]["expect"]["nsolutions"]
 
 
+@pytest.mark.parametrize("k", range(3))
+def test_dynamic_polynomials_18(k):
+    # test/solve_test.jl:338-344: f₁ = (x⁴ + y⁴ − 1)(x² + y² − 2) + x⁵y, f₂ = x² + 2xy² − 2y² − 1/2
+    # has 18 solutions (total degree 6·3 = 18: every path ends at a nonsingular solution), for
+    # any generic γ
+    H = hc.total_degree_homotopy(system("dynamic_polynomials_18"), np.exp(2j * np.pi * (0.13 + k / 3)))
+    res, *_ = track(H)
+    assert nonsingular(res) == KAT["dynamic_polynomials_18"]["expect"]["nsolutions"] == 18
+
+
 def test_valuation_examples():
     # test/valuation_test.jl:20-44 (Example 2) and :46-74 (Example 3), conservative parameters
     o = hco.default_options(beta_omega_p=4.0, beta_tau=0.25, strict_beta_tau=0.1875)
