@@ -16,6 +16,20 @@ def system(name):
                      [np.array([complex(*c) for c in cs]) for cs in d["coefficients"]], nvars=d["n"])
 
 
+def system_of(d):
+    """A System from a fixture dictionary (n, exponents, coefficients)."""
+    return hc.System([np.array(e, dtype=np.int32) for e in d["exponents"]],
+                     [np.array([complex(*c) for c in cs]) for cs in d["coefficients"]], nvars=d["n"])
+
+
+def straight_line_homotopy():
+    """The Tracker test's straight-line homotopy t G + (1 - t) F with its own start system G
+    (no total-degree scaling; γ = 1)."""
+    d = KAT["straight_line_tracker"]
+    F, G = system_of(d["F"]), system_of(d["G"])
+    return hc.systems.TotalDegreeHomotopy(F=F, G=G, gamma=1.0 + 0j, degrees=[2, 1], scaling=np.ones(2))
+
+
 def gamma(name):
     return complex(*KAT[name]["gamma"])
 

@@ -147,6 +147,27 @@ def main(ref):
                    r"@test_throws FiniteException\((\d+)\)", blk)
     out["parameter_solve"] = {"expect": {"nsolutions": int(n1.group(1)), "finite_exception_dim": int(fe.group(2))},
                               "underdetermined": to_param_system([fe.group(1)], ["x", "y"], ["a", "b"])}
+    # Beyond Polyhedral Homotopy Example: 2 successes, 2 at infinity (test/endgame_test.jl)
+    blk = en[en.index('@testset "Beyond Polyhedral Homotopy Example"'):]
+    fb = re.search(r"f = \[(.*?)\]\n", blk).group(1)
+    out["beyond_polyhedral"] = {**to_system(split_top_level(fb), ["x", "y"]), "expect": {
+        "success": int(re.search(r"count\(is_success, res\) == (\d+)", blk).group(1)),
+        "at_infinity": int(re.search(r"count\(is_at_infinity, res\) == (\d+)", blk).group(1))}}
+    # Tracker on a straight-line homotopy with a given start system (test/tracker_test.jl)
+    blk = tr[tr.index('@testset "Straight Line Homotopy"'):]
+    Fs = re.search(r"F = System\(\[(.*?)\], \[x, y\]\)", blk).group(1)
+    gm = re.search(r"G = System\(\(([^)]*)\) \.\* \[(.*?)\], \[x, y\]\)", blk)
+    starts = re.search(r"S = \[\[(.*?)\], \[(.*?)\]\]", blk)
+    bad = re.search(r"is_invalid_startvalue\(track\(tracker, \[(.*?)\], 1, 0\)\)", blk)
+    scale = complex(eval(julia_to_python(gm.group(1))))
+    G = to_system(split_top_level(gm.group(2)), ["x", "y"])
+    G["coefficients"] = [[[(complex(*c) * scale).real, (complex(*c) * scale).imag] for c in cs]
+                         for cs in G["coefficients"]]
+    out["straight_line_tracker"] = {"F": to_system(split_top_level(Fs), ["x", "y"]), "G": G,
+                                    "starts": [[float(v) for v in starts.group(1).split(",")],
+                                               [float(v) for v in starts.group(2).split(",")]],
+                                    "invalid_start": [float(v) for v in bad.group(1).split(",")],
+                                    "expect": {"starts": "success", "invalid_start": "terminated_invalid_startvalue"}}
     # solve (DynamicPolynomials): nsolutions == 18 (test/solve_test.jl)
     blk = sv[sv.index('@testset "solve (DynamicPolynomials)"'):]
     d1 = re.search(r"f₁ = (.*)\n", blk).group(1).strip()

@@ -84,6 +84,37 @@ def test_dynamic_polynomials_18(precision, step_control):
     assert_parity(ro, xo, rg, xg)
 
 
+@pytest.mark.parametrize("precision,step_control", MODES)
+def test_beyond_polyhedral_example(precision, step_control):
+    # test/endgame_test.jl:54-60: the 2×2 quadrics by total degree: 2 successes, 2 at infinity
+    e = KAT["beyond_polyhedral"]["expect"]
+    for k in range(3):
+        H = hc.total_degree_homotopy(system("beyond_polyhedral"), np.exp(2j * np.pi * (0.07 + k / 3)))
+        S = hc.total_degree_start_solutions(H.degrees)
+        ro, xo, _, _ = oracle_track(H, S)
+        (rg, xg, _, _), _ = gpu_track(H, S, precision, step_control)
+        codes = [hc.ENDGAME_CODES[int(c)] for c in rg["return_code"]]
+        assert codes.count("success") == e["success"] and codes.count("at_infinity") == e["at_infinity"]
+        assert_parity(ro, xo, rg, xg)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_straight_line_tracker(precision):
+    # test/tracker_test.jl:93-105: Tracker on t G + (1 - t) F from G's roots succeeds; from
+    # [100, -100] the start value is invalid (plain tracker, t from 1 to 0)
+    from _kat import straight_line_homotopy
+
+    d = KAT["straight_line_tracker"]
+    H = straight_line_homotopy()
+    S = np.array(d["starts"] + [d["invalid_start"]], dtype=np.complex128)
+    ro, xo, _, _ = oracle_track(H, S, endgame=False)
+    rg, xg, _, _ = hc.Tracker(H, hc.TrackerOptions(precision=precision)).track_arrays(S, t1=1.0, t0=0.0)
+    assert [hc.TRACKER_CODES[int(c)] for c in rg["return_code"]] == ["success", "success",
+                                                                     "terminated_invalid_startvalue"]
+    assert list(rg["return_code"]) == list(ro["return_code"])
+    assert rel_err(xg[:2], xo[:2]).max() <= REL_TOL
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_wilkinson_12(precision):
     # test/endgame_test.jl:38-45: roots 1..12 (only_nonsingular endgame), tiny imaginary parts.

@@ -80,6 +80,32 @@ def test_dynamic_polynomials_18(k):
     assert nonsingular(res) == KAT["dynamic_polynomials_18"]["expect"]["nsolutions"] == 18
 
 
+@pytest.mark.parametrize("k", range(3))
+def test_beyond_polyhedral_example(k):
+    # test/endgame_test.jl:54-60: the 2×2 quadrics by total degree: 2 successes, 2 at infinity
+    e = KAT["beyond_polyhedral"]["expect"]
+    H = hc.total_degree_homotopy(system("beyond_polyhedral"), np.exp(2j * np.pi * (0.07 + k / 3)))
+    res, *_ = track(H)
+    codes = [hc.ENDGAME_CODES[int(c)] for c in res["return_code"]]
+    assert codes.count("success") == e["success"] and codes.count("at_infinity") == e["at_infinity"]
+
+
+def test_straight_line_tracker():
+    # test/tracker_test.jl:93-105: Tracker on t G + (1 - t) F from G's roots succeeds; from
+    # [100, -100] (not a root of G) the start value is invalid
+    from _kat import straight_line_homotopy
+
+    d = KAT["straight_line_tracker"]
+    H = straight_line_homotopy()
+    S = np.array(d["starts"] + [d["invalid_start"]], dtype=np.complex128)
+    res, x, _, _ = track(H, S, endgame=False, t1=1.0, t0=0.0)
+    assert [hc.TRACKER_CODES[int(c)] for c in res["return_code"]] == ["success", "success",
+                                                                      "terminated_invalid_startvalue"]
+    F = H.F
+    for xi in x[:2]:
+        assert np.abs(F.evaluate(xi)).max() < 1e-12
+
+
 def test_valuation_examples():
     # test/valuation_test.jl:20-44 (Example 2) and :46-74 (Example 3), conservative parameters
     o = hco.default_options(beta_omega_p=4.0, beta_tau=0.25, strict_beta_tau=0.1875)
