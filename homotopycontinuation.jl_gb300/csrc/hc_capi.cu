@@ -682,6 +682,8 @@ int hc_default_options(hc_options* o) {
 
 // the GPU-side knobs of hc_options (the tracker parameters are the caller's to choose)
 static const char* invalid_knob(const hc_options* o) {
+  if (o->warps_per_cta < 0 || o->warps_per_cta > HC_MAX_WARPS) return "warps_per_cta must lie in [0, 16]";
+  if (o->ctas_per_sm < 0) return "ctas_per_sm must be >= 0";
   if (o->precision != HC_PREC_FP64 && o->precision != HC_PREC_MIXED) return "unknown precision";
   if (o->step_control != HC_STEP_PLAIN && o->step_control != HC_STEP_LEARNED && o->step_control != HC_STEP_EXPLORE)
     return "unknown step control";
@@ -1004,11 +1006,17 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
 //   2,000 uneven instances (batch), mixed + learned, 8 warps  61.6k | 89.2k  73.9k  85.6k
 // The warps share the instruction cache when they run the same code; with 4 or 5 warps the
 // waits cost more than that gains.
-static int lockstep_for(const hc_options& O, int wpc, bool batch = false) {
+// With up to 16 warps per CTA (CTA-wide lockstep; 8 warps → the most that fit): 6 dense cubics,
+// mixed + plain, 100k → 115k (16 warps); 7 dense cubics 72k → 90k (16); 8 dense cubics 58.8k →
+// 68.6k (13); 8 sparse quartics, mixed + learned, 20.4k → 22.2k (12), FP64 + learned 23.2k →
+// 23.6k (11). On those smaller programs the CTA-wide barrier beats the groups of four (8 dense
+// cubics at 8 warps 58.8k vs 54.7k, 6 dense cubics 100k vs 74k); the groups win on the 10 dense
+// cubics (2,880 value terms).
+static int lockstep_for(const hc_options& O, int wpc, bool batch = false, long long value_terms = 0) {
   if (O.lockstep >= 0) return O.lockstep;
   if (batch) return wpc >= 8 ? 1 : 0;
-  if (O.precision == HC_PREC_MIXED) return wpc >= 8 ? 3 : (wpc >= 6 ? 2 : 0);
-  return wpc >= 8 ? 1 : 0;
+  if (wpc >= 8) return O.precision == HC_PREC_MIXED && value_terms >= 2000 ? 3 : 1;
+  return O.precision == HC_PREC_MIXED && wpc >= 6 ? 2 : 0;
 }
 
 // Mixed precision: 5 warps per CTA (two sub-partitions with two warps, two with one) measured
@@ -1080,11 +1088,11 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   la.tor_w = pa.tor_w;
   la.tor_row = pa.tor_row;
   if (la.log) CK(cudaMemsetAsync(h->d_log_count, 0, sizeof(unsigned long long), s));
-  // warps per CTA: as many as fit next to one copy of the tables (capped at 8)
+  // warps per CTA: as many as fit next to one copy of the tables (capped at HC_MAX_WARPS)
   const size_t smem_cap = 227 * 1024;
   int wpc = O.warps_per_cta;
   if (wpc <= 0) {
-    wpc = (int)std::min<size_t>(8, (smem_cap - la.T.bytes) / la.L.bytes);
+    wpc = (int)std::min<size_t>(HC_MAX_WARPS, (smem_cap - la.T.bytes) / la.L.bytes);
     wpc = std::max(wpc, 1);
     wpc = balanced_warps(wpc, O.precision);
   }
@@ -1093,7 +1101,7 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
     --wpc;
     smem = (size_t)la.T.bytes + (size_t)wpc * la.L.bytes;
   }
-  la.lockstep = lockstep_for(O, wpc);
+  la.lockstep = lockstep_for(O, wpc, false, h->prog.val_terms);
   h->last_lockstep = la.lockstep;
   int bps = 0;
   cudaKernel_t jit = nullptr;  // the NVRTC kernel of a straight-line program
@@ -1682,7 +1690,7 @@ static int batch_geometry(hc_handle* h, const hc_options& O, int nunits, size_t*
   const int q = O.precision == HC_PREC_MIXED ? 1 : 0;
   const size_t smem_cap = 227 * 1024;
   const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
-  int wpc = O.warps_per_cta;
+  int wpc = std::min(O.warps_per_cta, HC_MAX_BATCH_WARPS);  // the batch kernel runs at most 8
   if (wpc <= 0)
     wpc = balanced_warps((int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride[q])),
                          O.precision);
@@ -2147,8 +2155,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
     return fail(h, HC_ERR_UNSUPPORTED, "hc_track_noalloc: learned step control needs a handle (hc_set_step_model)");
   if (opts->step_control != HC_STEP_PLAIN && opts->step_control != HC_STEP_EXPLORE)
     return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: unknown step control");
-  if (opts->lockstep < -1 || opts->lockstep > 3)
-    return fail(h, HC_ERR_INVALID_ARG, "hc_track_noalloc: lockstep must be -1, 0, 1, 2 or 3");
+  if (invalid_knob(opts)) return fail(h, HC_ERR_INVALID_ARG, std::string("hc_track_noalloc: ") + invalid_knob(opts));
   {
     // The compiled tables are copied from a host buffer that lives only for this call; a
     // copy recorded into a graph would read it after it is freed. Checked before any other
@@ -2233,7 +2240,7 @@ extern "C" int hc_track_noalloc(const hc_options* opts, int n, int nG, const int
     smem = (size_t)T.bytes + (size_t)wpc * L.bytes;
   }
   if (smem > smem_cap) return fail(h, HC_ERR_TOO_LARGE, "hc_track_noalloc: working set exceeds shared memory");
-  la.lockstep = lockstep_for(*opts, wpc);
+  la.lockstep = lockstep_for(*opts, wpc, false, P.val_terms);
   int bps = 0;
   e = occupancy(opts->precision, wpc, smem, &bps);
   if (e != cudaSuccess) return cuda_fail(h, e, "hc_track_noalloc: occupancy");

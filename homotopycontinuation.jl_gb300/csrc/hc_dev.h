@@ -152,5 +152,8 @@ struct BatchLaunch {
   int wstride;  // shared bytes per warp (maximum over the instances)
 };
 constexpr int HC_LAUNCH_SMEM = (int)((sizeof(Launch) + 127) & ~(size_t)127);
+// warps per CTA at most: the single-homotopy kernel (track_kernel) and the batch kernel
+constexpr int HC_MAX_WARPS = 16;
+constexpr int HC_MAX_BATCH_WARPS = 8;
 
 }  // namespace hcd

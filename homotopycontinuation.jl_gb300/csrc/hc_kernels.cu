@@ -9,7 +9,7 @@ namespace hcd {
 // instance's tables, warps track the unit's paths, and a barrier closes the unit before the
 // tables are overwritten. Paths are numbered within their instance (path_number = k + 1).
 template <bool MIXED>
-__global__ void __launch_bounds__(256) track_batch_kernel(const __grid_constant__ BatchLaunch bl) {
+__global__ void __launch_bounds__(HC_MAX_BATCH_WARPS * 32) track_batch_kernel(const __grid_constant__ BatchLaunch bl) {
   extern __shared__ __align__(16) char smem[];
   __shared__ int s_unit;
   __shared__ unsigned s_next;

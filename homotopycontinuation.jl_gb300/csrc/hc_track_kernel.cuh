@@ -67,7 +67,7 @@ __device__ __forceinline__ void add_phases(unsigned long long* ph, const PathTra
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) track_kernel(const __grid_constant__ Launch la) {
+__global__ void __launch_bounds__(HC_MAX_WARPS * 32) track_kernel(const __grid_constant__ Launch la) {
   static_assert(sizeof(PathTracker<MIXED>) <= HC_STATE_BYTES, "tracker state exceeds its shared-memory slot");
   extern __shared__ __align__(16) char smem[];
   const TableLayout& TL = la.T;
