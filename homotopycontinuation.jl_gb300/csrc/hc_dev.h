@@ -62,7 +62,13 @@ struct WarpLayout {
   // area at cmono and the partial sums at cpart. cold == 0: those areas alias mono and part.
   int cold, cmono, cpart;
 };
-constexpr int HC_STATE_BYTES = 2048;  // per-warp tracker state object
+// per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
+// counters of profiling builds)
+#ifdef HC_PHASE_CLOCKS
+constexpr int HC_STATE_BYTES = 1536;
+#else
+constexpr int HC_STATE_BYTES = 1280;
+#endif
 constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
 constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
 constexpr int HC_NFEAT = 12;       // step features of the learned proposal
@@ -73,6 +79,7 @@ constexpr int HC_NSTATS = 11;      // device counters of a tracking call
 enum HcPhase {
   PH_RUN, PH_STEP, PH_PREDICTOR, PH_PREDICT, PH_NEWTON, PH_EVALJ, PH_EVAL, PH_TAYLOR, PH_LU, PH_SOLVE,
   PH_NORM, PH_STEPSIZE, PH_ENDGAME, PH_MONO, PH_VALROWS, PH_JACROWS, PH_REFINE, PH_INIT, PH_COND, PH_DD,
+  PH_WAIT,  // lockstep schedules: waits at the round barrier (PH_RUN then spans the warp's whole loop)
   HC_NPHASE
 };
 

@@ -118,6 +118,9 @@ __global__ void __launch_bounds__(HC_MAX_WARPS * 32) track_kernel(const __grid_c
     // Every warp reaches the barrier once per round and all leave together.
     bool active = false, done = false;
     int64_t kk = 0;
+#ifdef HC_PHASE_CLOCKS
+    const long long t_run = clock64();
+#endif
     while (true) {
       if (!active && !done) {
         if (!take(kk)) {
@@ -137,8 +140,18 @@ __global__ void __launch_bounds__(HC_MAX_WARPS * 32) track_kernel(const __grid_c
         active = false;
         ++npaths_done;
       }
+#ifdef HC_PHASE_CLOCKS
+      const long long t_wait = clock64();
+      const bool all_done = lockstep_round(la.lockstep, done && !active);
+      if (lane == 0) T->ph[PH_WAIT] += (unsigned long long)(clock64() - t_wait);
+      if (all_done) break;
+#else
       if (lockstep_round(la.lockstep, done && !active)) break;
+#endif
     }
+#ifdef HC_PHASE_CLOCKS
+    if (lane == 0) T->ph[PH_RUN] += (unsigned long long)(clock64() - t_run);
+#endif
   }
   __syncwarp();
   if (lane == 0 && la.stats) add_stats(la.stats, T, npaths_done);

@@ -264,7 +264,7 @@ class _Handle:
                   "smem_per_warp", "smem_tables", "top", "learned_proposals", "learned_rejected"] + [
         "clk_" + p for p in ("run", "step", "predictor", "predict", "newton", "eval_jac", "eval", "taylor", "lu",
                              "solve", "norm", "stepsize", "endgame", "mono", "val_rows", "jac_rows", "refine",
-                             "init", "cond", "dd")] + ["paths_retracked", "lockstep"]
+                             "init", "cond", "dd", "wait")] + ["paths_retracked", "lockstep"]
 
     def stats(self):
         out = np.zeros(len(self.STAT_NAMES))

@@ -198,7 +198,7 @@ int hc_slp_parameter_source(const hc_slp* F, int nparameters, int32_t parameters
  * Copies in, runs and copies out on the handle's stream; returns when the results are on the host.
  * With learned step control (and the endgame), paths whose nonsingular endpoints coincide with
  * another path's — the mark of a path that jumped onto another path — are re-tracked in place
- * with the plain step rule before returning (hc_last_stats [39] counts them); the device entry
+ * with the plain step rule before returning (hc_last_stats [40] counts them); the device entry
  * points return the tracker's results unchecked. */
 int hc_track(hc_handle* h, int64_t npaths, const double* starts, int endgame, double t1_re,
              double t1_im, double t0_re, double t0_im, hc_path_result* out_results,
@@ -268,11 +268,12 @@ const char* hc_last_error(hc_handle* h);
  * evaluations redone in FP64, [8] paths moved to FP64; [9] monomials, [10] value terms,
  * [11] Jacobian terms of the last hc_set_homotopy program; [12] CTAs, [13] warps per CTA,
  * [14] shared bytes per warp, [15] shared bytes of the CTA tables, [16] top-degree monomial
- * offset; [17] learned step proposals, [18] of them rejected by Newton; [19..38] cycles per
+ * offset; [17] learned step proposals, [18] of them rejected by Newton; [19..39] cycles per
  * tracker phase (run, step, predictor, predict, newton, eval+Jacobian, eval, taylor, LU,
  * solve, norm, step size, endgame, monomials, value rows, Jacobian rows, refinement, init,
- * cond, double-double; inclusive), nonzero only in libraries built with -DHC_PHASE_CLOCKS;
- * [39] paths re-tracked with plain step control by the jump check of hc_track/hc_track_batch.
+ * cond, double-double, lockstep barrier waits; inclusive), nonzero only in libraries built with
+ * -DHC_PHASE_CLOCKS; [40] paths re-tracked with plain step control by the jump check of
+ * hc_track/hc_track_batch; [41] lockstep mode of the last launch (hc_options::lockstep).
  * No counterpart in the reference (its closest analogue is the Jacobian's factorization and
  * ldiv counters, src/linear_algebra.jl:809-862). */
 int hc_last_stats(hc_handle* h, double* out, int nout);
