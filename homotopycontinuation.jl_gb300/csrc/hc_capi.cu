@@ -1508,9 +1508,11 @@ static std::vector<BatchUnit> batch_units(const hc_handle* h, const int32_t* uni
   return out;
 }
 
-// warps per CTA the default unit size assumes (shared-memory fit of the mixed tables, at most 8)
+// warps per CTA the default unit size assumes (shared-memory fit of the mixed tables, at most
+// HC_MAX_BATCH_WARPS)
 static int batch_wpc_estimate(int tb, int ws) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>(8, (227 * 1024 - HC_LAUNCH_SMEM - tb) / std::max(ws, 1)));
+  return (int)std::max<int64_t>(
+      1, std::min<int64_t>(HC_MAX_BATCH_WARPS, (227 * 1024 - HC_LAUNCH_SMEM - tb) / std::max(ws, 1)));
 }
 
 // upload `units` into a device array of the handle (grown on demand)
@@ -1690,10 +1692,11 @@ static int batch_geometry(hc_handle* h, const hc_options& O, int nunits, size_t*
   const int q = O.precision == HC_PREC_MIXED ? 1 : 0;
   const size_t smem_cap = 227 * 1024;
   const size_t fixed = (size_t)HC_LAUNCH_SMEM + h->btbytes[q];
-  int wpc = std::min(O.warps_per_cta, HC_MAX_BATCH_WARPS);  // the batch kernel runs at most 8
+  int wpc = std::min(O.warps_per_cta, HC_MAX_BATCH_WARPS);
   if (wpc <= 0)
-    wpc = balanced_warps((int)std::max<size_t>(1, std::min<size_t>(8, (smem_cap - fixed) / h->bwstride[q])),
-                         O.precision);
+    wpc = balanced_warps(
+        (int)std::max<size_t>(1, std::min<size_t>(HC_MAX_BATCH_WARPS, (smem_cap - fixed) / h->bwstride[q])),
+        O.precision);
   size_t smem = fixed + (size_t)wpc * h->bwstride[q];
   while (wpc > 1 && smem > smem_cap) {
     --wpc;

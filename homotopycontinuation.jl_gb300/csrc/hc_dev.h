@@ -161,6 +161,6 @@ struct BatchLaunch {
 constexpr int HC_LAUNCH_SMEM = (int)((sizeof(Launch) + 127) & ~(size_t)127);
 // warps per CTA at most: the single-homotopy kernel (track_kernel) and the batch kernel
 constexpr int HC_MAX_WARPS = 16;
-constexpr int HC_MAX_BATCH_WARPS = 8;
+constexpr int HC_MAX_BATCH_WARPS = 16;
 
 }  // namespace hcd

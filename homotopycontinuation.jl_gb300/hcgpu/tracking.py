@@ -56,7 +56,7 @@ class TrackerOptions:
     precision: str = "fp64"  # "fp64" | "mixed"
     step_control: str = "plain"  # "plain" | "learned" | "explore"
     step_model: Optional[object] = None  # learn.StepModel for "learned"; None: the shipped model
-    warps_per_cta: int = 0  # 0: as many as fit in shared memory (at most 16, batches 8)
+    warps_per_cta: int = 0  # 0: as many as fit in shared memory (at most 16)
     ctas_per_sm: int = 0
     lockstep: int = -1  # lockstep of a CTA's warps: 1 all, 2 per sub-partition, 3 per two, 0 none, -1 auto
 

@@ -68,14 +68,14 @@ typedef struct hc_options {
   /* GPU-side knobs (no counterpart in the reference) */
   int32_t precision;      /* enum hc_precision */
   int32_t step_control;   /* enum hc_step_control */
-  int32_t warps_per_cta;  /* 0 = as many as fit in shared memory (at most 16; batches at most 8), 1..16 */
+  int32_t warps_per_cta;  /* 0 = as many as fit in shared memory (at most 16), 1..16 */
   int32_t ctas_per_sm;    /* 0 = as many as fit */
   /* scheduling of a CTA's warps: 1 = lockstep (every warp advances its path by one step, then
    * the CTA waits for all, so the warps run the same code together and share the instruction
    * cache), 2 = lockstep of the warps that share an SM sub-partition (warps w, w + 4), 3 = of the
    * warps of two sub-partitions, 0 = each warp on its own, -1 = automatic (1 with 8 or more
    * warps per CTA, except 3 for mixed-precision homotopies of 2,000 value terms or more; 2 for
-   * mixed precision with 6 or 7 warps; batches 1 with 8). Results are identical in every mode. */
+   * mixed precision with 6 or 7 warps; batches 1 with 8 or more). Results are identical in every mode. */
   int32_t lockstep;
   int32_t reserved;
 } hc_options;
