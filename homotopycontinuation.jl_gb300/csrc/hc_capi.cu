@@ -413,7 +413,12 @@ WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0, bool cold = false)
   L.xJ = take((size_t)vn * 16);
   L.dinv = take((size_t)vn * 16);
   L.ipiv = take(32 * 4);
-  L.vec = take((size_t)HC_NCVEC * vn * 16);
+  L.vec = take((size_t)(cold ? HC_NCVEC - HC_NCVEC_COLD : HC_NCVEC) * vn * 16);
+  L.cvec = -1;
+  if (cold) {
+    L.cvec = L.cold;
+    L.cold += (int)up16((size_t)HC_NCVEC_COLD * vn * 16);
+  }
   L.rvec = take((size_t)HC_NRVEC * vn * 8);
   L.v32 = take((size_t)4 * vn * 8);
   L.tor = tor_n > 0 ? take((size_t)tor_n * (16 + 8 + 8)) : 0;

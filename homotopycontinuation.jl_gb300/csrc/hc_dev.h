@@ -61,6 +61,10 @@ struct WarpLayout {
   // global memory (Launch::cold) instead of shared memory: `cold` bytes per warp, the monomial
   // area at cmono and the partial sums at cpart. cold == 0: those areas alias mono and part.
   int cold, cmono, cpart;
+  // cold layout: the last HC_NCVEC_COLD complex vectors (endgame predictions and the singular
+  // endgame's samples, used once per endgame step or less) at this offset of the global slice
+  // instead of shared memory; −1: all HC_NCVEC vectors in shared memory
+  int cvec;
 };
 // per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
 // counters of profiling builds)
@@ -69,7 +73,7 @@ constexpr int HC_STATE_BYTES = 1536;
 #else
 constexpr int HC_STATE_BYTES = 1280;
 #endif
-constexpr int HC_NCVEC = 24, HC_NRVEC = 20;
+constexpr int HC_NCVEC = 24, HC_NRVEC = 20, HC_NCVEC_COLD = 9;
 constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
 constexpr int HC_NFEAT = 12;       // step features of the learned proposal
 constexpr int HC_NSTATS = 11;      // device counters of a tracking call

@@ -268,10 +268,12 @@ struct PathTracker {
     mdef = (const int2*)(tbase + TL.mdef);
     mono64 = (c64*)(base + L.mono);
     part = base + L.part;
+    c64* cv_end = nullptr;  // the vectors from lastp on (HC_NCVEC_COLD of them)
     if (L.cold > 0 && la->cold) {
       char* cb = la->cold + (size_t)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * (size_t)L.cold;
       mono_c = cb + L.cmono;
       part_c = cb + L.cpart;
+      if (L.cvec >= 0) cv_end = (c64*)(cb + L.cvec);
     } else {
       mono_c = (char*)mono64;
       part_c = part;
@@ -297,10 +299,12 @@ struct PathTracker {
     ptx1 = cv + 12 * vn;
     u = cv + 13 * vn;
     sol = cv + 14 * vn;
-    lastp = cv + 15 * vn;
-    pred = cv + 16 * vn;
-    ppred = cv + 17 * vn;
-    smp = cv + 18 * vn;  // 6 vectors
+    static_assert(HC_NCVEC - HC_NCVEC_COLD == 15, "lastp .. smp are the vectors a cold layout moves");
+    if (!cv_end) cv_end = cv + 15 * vn;
+    lastp = cv_end + 0 * vn;
+    pred = cv_end + 1 * vn;
+    ppred = cv_end + 2 * vn;
+    smp = cv_end + 3 * vn;  // 6 vectors
     double* rv = (double*)(base + L.rvec);
     w = rv + 0 * vn;
     rs = rv + 1 * vn;
