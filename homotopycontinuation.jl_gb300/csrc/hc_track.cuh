@@ -180,11 +180,11 @@ struct PathTracker {
   c32* v32;   // FP32 staging vectors (4 × vn)
   int* ipiv;
   // complex vectors
-  c64 *x, *xh, *xb, *r, *s1, *s2, *s3, *tx0, *tx1, *tx2, *tx3, *ptx0, *ptx1, *u;
+  c64 *x, *xh, *xb, *r, *s1, *s2, *tx0, *tx1, *tx2, *tx3, *ptx0, *ptx1, *u;
   c64 *sol, *lastp, *pred, *ppred, *smp;
   // real vectors
   double *w, *winv, *rs, *egrs, *egcs, *ais, *ait, *aia, *aic, *vx, *vtx, *dvx, *dvtx, *nu2, *nu1, *lx2, *lx1,
-      *lxd2, *lxd1, *rtmp;
+      *lxd2, *lxd1;
 
   // ---- MatrixWorkspace state (src/linear_algebra.jl:7-22)
   bool factorized, scaled;
@@ -290,17 +290,16 @@ struct PathTracker {
     r = cv + 3 * vn;
     s1 = cv + 4 * vn;
     s2 = cv + 5 * vn;
-    s3 = cv + 6 * vn;
-    tx0 = cv + 7 * vn;
-    tx1 = cv + 8 * vn;
-    tx2 = cv + 9 * vn;
-    tx3 = cv + 10 * vn;
-    ptx0 = cv + 11 * vn;
-    ptx1 = cv + 12 * vn;
-    u = cv + 13 * vn;
-    sol = cv + 14 * vn;
-    static_assert(HC_NCVEC - HC_NCVEC_COLD == 15, "lastp .. smp are the vectors a cold layout moves");
-    if (!cv_end) cv_end = cv + 15 * vn;
+    tx0 = cv + 6 * vn;
+    tx1 = cv + 7 * vn;
+    tx2 = cv + 8 * vn;
+    tx3 = cv + 9 * vn;
+    ptx0 = cv + 10 * vn;
+    ptx1 = cv + 11 * vn;
+    u = cv + 12 * vn;
+    sol = cv + 13 * vn;
+    static_assert(HC_NCVEC - HC_NCVEC_COLD == 14, "lastp .. smp are the vectors a cold layout moves");
+    if (!cv_end) cv_end = cv + 14 * vn;
     lastp = cv_end + 0 * vn;
     pred = cv_end + 1 * vn;
     ppred = cv_end + 2 * vn;
@@ -324,8 +323,7 @@ struct PathTracker {
     lx1 = rv + 15 * vn;
     lxd2 = rv + 16 * vn;
     lxd1 = rv + 17 * vn;
-    rtmp = rv + 18 * vn;
-    winv = rv + 19 * vn;
+    winv = rv + 18 * vn;
     dinv = (c64*)(base + L.dinv);
     v32 = (c32*)(base + L.v32);
     toric = !MIXED && la->tor_w != nullptr && L.tor_n > 0;
