@@ -95,6 +95,13 @@ def test_lockstep_in_batches():
     r, x = B.track_arrays()
     _same(res[0][0], res[0][1], r, x)
     assert B.stats()["lockstep"] == (1 if B.stats()["warps_per_block"] >= 8 else 0)
+    # more than 8 warps per CTA (as many as fit, at most 16) against 8 and 4: the same results
+    assert B.stats()["warps_per_block"] > 8
+    for w in (8, 4):
+        Bw = hc.BatchTracker(Hs, hc.TrackerOptions(precision="mixed", step_control="learned", warps_per_cta=w))
+        rw, xw = Bw.track_arrays()
+        assert Bw.stats()["warps_per_block"] == w
+        _same(r, x, rw, xw)
 
 
 def test_lockstep_option_is_validated():
