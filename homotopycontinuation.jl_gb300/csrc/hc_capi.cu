@@ -410,16 +410,20 @@ WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0, bool cold = false)
   }
   L.A = take((size_t)n * n * 16);
   L.LU = take((size_t)n * n * 16);
-  L.xJ = take((size_t)vn * 16);
+  L.xJ = cold ? 0 : take((size_t)vn * 16);
   L.dinv = take((size_t)vn * 16);
-  L.ipiv = take(32 * 4);
+  L.ipiv = take(64);  // row permutation and its inverse, one byte per row
   L.vec = take((size_t)(cold ? HC_NCVEC - HC_NCVEC_COLD : HC_NCVEC) * vn * 16);
-  L.cvec = -1;
+  L.rvec = take((size_t)(cold ? HC_NRVEC - HC_NRVEC_COLD : HC_NRVEC) * vn * 8);
+  L.cvec = L.crvec = L.cxj = -1;
   if (cold) {
     L.cvec = L.cold;
     L.cold += (int)up16((size_t)HC_NCVEC_COLD * vn * 16);
+    L.crvec = L.cold;
+    L.cold += (int)up16((size_t)HC_NRVEC_COLD * vn * 8);
+    L.cxj = L.cold;
+    L.cold += (int)up16((size_t)vn * 16);
   }
-  L.rvec = take((size_t)HC_NRVEC * vn * 8);
   L.v32 = take((size_t)4 * vn * 8);
   L.tor = tor_n > 0 ? take((size_t)tor_n * (16 + 8 + 8)) : 0;
   L.tor_n = tor_n;

@@ -61,10 +61,12 @@ struct WarpLayout {
   // global memory (Launch::cold) instead of shared memory: `cold` bytes per warp, the monomial
   // area at cmono and the partial sums at cpart. cold == 0: those areas alias mono and part.
   int cold, cmono, cpart;
-  // cold layout: the last HC_NCVEC_COLD complex vectors (endgame predictions and the singular
-  // endgame's samples, used once per endgame step or less) at this offset of the global slice
-  // instead of shared memory; −1: all HC_NCVEC vectors in shared memory
-  int cvec;
+  // cold layout: the last HC_NCVEC_COLD complex vectors (the endgame's solution estimate and
+  // predictions and the singular endgame's samples), the last HC_NRVEC_COLD real vectors (the
+  // endgame's scalings, condition estimates and valuation) and the point of the last Jacobian
+  // (xJ) — each used once per endgame step or evaluation or less — at these offsets of the
+  // global slice instead of shared memory; −1: in shared memory
+  int cvec, crvec, cxj;
 };
 // per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
 // counters of profiling builds)
@@ -73,7 +75,7 @@ constexpr int HC_STATE_BYTES = 1536;
 #else
 constexpr int HC_STATE_BYTES = 1280;
 #endif
-constexpr int HC_NCVEC = 23, HC_NRVEC = 19, HC_NCVEC_COLD = 9;
+constexpr int HC_NCVEC = 23, HC_NRVEC = 19, HC_NCVEC_COLD = 10, HC_NRVEC_COLD = 16;
 constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
 constexpr int HC_NFEAT = 12;       // step features of the learned proposal
 constexpr int HC_NSTATS = 11;      // device counters of a tracking call

@@ -268,19 +268,25 @@ struct PathTracker {
     mdef = (const int2*)(tbase + TL.mdef);
     mono64 = (c64*)(base + L.mono);
     part = base + L.part;
-    c64* cv_end = nullptr;  // the vectors from lastp on (HC_NCVEC_COLD of them)
+    // the vectors a cold layout keeps in the warp's global slice: complex from sol on
+    // (HC_NCVEC_COLD), real from egrs on (HC_NRVEC_COLD), and xJ
+    c64* cv_end = nullptr;
+    double* rv_end = nullptr;
+    xJ = nullptr;
     if (L.cold > 0 && la->cold) {
       char* cb = la->cold + (size_t)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * (size_t)L.cold;
       mono_c = cb + L.cmono;
       part_c = cb + L.cpart;
       if (L.cvec >= 0) cv_end = (c64*)(cb + L.cvec);
+      if (L.crvec >= 0) rv_end = (double*)(cb + L.crvec);
+      if (L.cxj >= 0) xJ = (c64*)(cb + L.cxj);
     } else {
       mono_c = (char*)mono64;
       part_c = part;
     }
     Ab = base + L.A;
     LUb = base + L.LU;
-    xJ = (c64*)(base + L.xJ);
+    if (!xJ) xJ = (c64*)(base + L.xJ);
     ipiv = (int*)(base + L.ipiv);
     c64* cv = (c64*)(base + L.vec);
     const int vn = L.vn;
@@ -297,33 +303,35 @@ struct PathTracker {
     ptx0 = cv + 10 * vn;
     ptx1 = cv + 11 * vn;
     u = cv + 12 * vn;
-    sol = cv + 13 * vn;
-    static_assert(HC_NCVEC - HC_NCVEC_COLD == 14, "lastp .. smp are the vectors a cold layout moves");
-    if (!cv_end) cv_end = cv + 14 * vn;
-    lastp = cv_end + 0 * vn;
-    pred = cv_end + 1 * vn;
-    ppred = cv_end + 2 * vn;
-    smp = cv_end + 3 * vn;  // 6 vectors
+    static_assert(HC_NCVEC - HC_NCVEC_COLD == 13, "sol .. smp are the vectors a cold layout moves");
+    if (!cv_end) cv_end = cv + 13 * vn;
+    sol = cv_end + 0 * vn;
+    lastp = cv_end + 1 * vn;
+    pred = cv_end + 2 * vn;
+    ppred = cv_end + 3 * vn;
+    smp = cv_end + 4 * vn;  // 6 vectors
     double* rv = (double*)(base + L.rvec);
     w = rv + 0 * vn;
     rs = rv + 1 * vn;
-    egrs = rv + 2 * vn;
-    egcs = rv + 3 * vn;
-    ais = rv + 4 * vn;
-    ait = rv + 5 * vn;
-    aia = rv + 6 * vn;
-    aic = rv + 7 * vn;
-    vx = rv + 8 * vn;
-    vtx = rv + 9 * vn;
-    dvx = rv + 10 * vn;
-    dvtx = rv + 11 * vn;
-    nu2 = rv + 12 * vn;
-    nu1 = rv + 13 * vn;
-    lx2 = rv + 14 * vn;
-    lx1 = rv + 15 * vn;
-    lxd2 = rv + 16 * vn;
-    lxd1 = rv + 17 * vn;
-    winv = rv + 18 * vn;
+    winv = rv + 2 * vn;
+    static_assert(HC_NRVEC - HC_NRVEC_COLD == 3, "egrs .. lxd1 are the vectors a cold layout moves");
+    if (!rv_end) rv_end = rv + 3 * vn;
+    egrs = rv_end + 0 * vn;
+    egcs = rv_end + 1 * vn;
+    ais = rv_end + 2 * vn;
+    ait = rv_end + 3 * vn;
+    aia = rv_end + 4 * vn;
+    aic = rv_end + 5 * vn;
+    vx = rv_end + 6 * vn;
+    vtx = rv_end + 7 * vn;
+    dvx = rv_end + 8 * vn;
+    dvtx = rv_end + 9 * vn;
+    nu2 = rv_end + 10 * vn;
+    nu1 = rv_end + 11 * vn;
+    lx2 = rv_end + 12 * vn;
+    lx1 = rv_end + 13 * vn;
+    lxd2 = rv_end + 14 * vn;
+    lxd1 = rv_end + 15 * vn;
     dinv = (c64*)(base + L.dinv);
     v32 = (c32*)(base + L.v32);
     toric = !MIXED && la->tor_w != nullptr && L.tor_n > 0;
