@@ -408,15 +408,19 @@ WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0, bool cold = false)
     L.mono = take(mono_all);
     L.part = take(part_all);
   }
-  L.A = take((size_t)n * n * 16);
-  L.LU = take((size_t)n * n * 16);
+  L.A = take((size_t)n * n * (cold ? 8 : 16));
+  L.LU = take((size_t)n * n * (cold ? 8 : 16));
   L.xJ = cold ? 0 : take((size_t)vn * 16);
   L.dinv = take((size_t)vn * 16);
   L.ipiv = take(64);  // row permutation and its inverse, one byte per row
   L.vec = take((size_t)(cold ? HC_NCVEC - HC_NCVEC_COLD : HC_NCVEC) * vn * 16);
   L.rvec = take((size_t)(cold ? HC_NRVEC - HC_NRVEC_COLD : HC_NRVEC) * vn * 8);
-  L.cvec = L.crvec = L.cxj = -1;
+  L.cvec = L.crvec = L.cxj = L.cA = L.cLU = -1;
   if (cold) {
+    L.cA = L.cold;
+    L.cold += (int)up16((size_t)n * n * 16);
+    L.cLU = L.cold;
+    L.cold += (int)up16((size_t)n * n * 16);
     L.cvec = L.cold;
     L.cold += (int)up16((size_t)HC_NCVEC_COLD * vn * 16);
     L.crvec = L.cold;

@@ -67,6 +67,10 @@ struct WarpLayout {
   // (xJ) — each used once per endgame step or evaluation or less — at these offsets of the
   // global slice instead of shared memory; −1: in shared memory
   int cvec, crvec, cxj;
+  // cold layout: A and LU in shared memory hold FP32 entries only (mixed precision's Jacobian);
+  // FP64 Jacobians (path starts, condition numbers, the FP64 fallback) use A and LU at these
+  // offsets of the global slice; −1: one shared A and LU of FP64 size serve both arithmetics
+  int cA, cLU;
 };
 // per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
 // counters of profiling builds)

@@ -173,8 +173,9 @@ struct PathTracker {
   // with the cold layout, else the same shared areas as mono64 / part
   char* mono_c;
   char* part_c;
-  char* Ab;
+  char* Ab;   // A and LU of the current Jacobian's arithmetic (Aprec): Ab64/LUb64 or Ab32/LUb32
   char* LUb;
+  char *Ab64, *LUb64, *Ab32, *LUb32;
   c64* xJ;
   c64* dinv;  // reciprocals of U's diagonal, stored in the LU's arithmetic (c64 or c32)
   c32* v32;   // FP32 staging vectors (4 × vn)
@@ -273,6 +274,7 @@ struct PathTracker {
     c64* cv_end = nullptr;
     double* rv_end = nullptr;
     xJ = nullptr;
+    Ab64 = LUb64 = nullptr;
     if (L.cold > 0 && la->cold) {
       char* cb = la->cold + (size_t)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * (size_t)L.cold;
       mono_c = cb + L.cmono;
@@ -280,12 +282,18 @@ struct PathTracker {
       if (L.cvec >= 0) cv_end = (c64*)(cb + L.cvec);
       if (L.crvec >= 0) rv_end = (double*)(cb + L.crvec);
       if (L.cxj >= 0) xJ = (c64*)(cb + L.cxj);
+      if (L.cA >= 0) Ab64 = cb + L.cA;
+      if (L.cLU >= 0) LUb64 = cb + L.cLU;
     } else {
       mono_c = (char*)mono64;
       part_c = part;
     }
-    Ab = base + L.A;
-    LUb = base + L.LU;
+    Ab32 = base + L.A;
+    LUb32 = base + L.LU;
+    if (!Ab64) Ab64 = Ab32;
+    if (!LUb64) LUb64 = LUb32;
+    Ab = Ab64;
+    LUb = LUb64;
     if (!xJ) xJ = (c64*)(base + L.xJ);
     ipiv = (int*)(base + L.ipiv);
     c64* cv = (c64*)(base + L.vec);
@@ -699,6 +707,9 @@ struct PathTracker {
   template <class T>
   __device__ HC_NI void H_eval_jac(const c64* xv, c64 t) {
     HC_PHASE(PH_EVALJ);
+    // the A and LU of this arithmetic (the cold layout keeps the FP64 ones in global memory)
+    Ab = std::is_same<T, c32>::value ? Ab32 : Ab64;
+    LUb = std::is_same<T, c32>::value ? LUb32 : LUb64;
 #ifdef HC_SLP
     slp_H_eval_jac<T>(xv, t);
 #else
