@@ -399,8 +399,9 @@ WarpLayout make_warp_layout(const HostProg& P, int tor_n = 0, bool cold = false)
   size_t mono_all = std::max({(size_t)P.M * 32, (size_t)P.M * 24, series});
   size_t part_all = std::max({(size_t)P.val.nslots * 32, (size_t)P.jac.nslots * 16, (size_t)16});
   if (cold) {
+    L.jmono = (size_t)P.jac.nslots * 8 <= (size_t)P.M * 16 ? 1 : 0;
     L.mono = take(std::max({(size_t)P.M * 24, series / 2, (size_t)16}));
-    L.part = take(std::max({(size_t)P.val.nslots * 24, (size_t)P.jac.nslots * 8, (size_t)16}));
+    L.part = take(std::max({(size_t)P.val.nslots * 24, L.jmono ? (size_t)0 : (size_t)P.jac.nslots * 8, (size_t)16}));
     L.cmono = 0;
     L.cpart = (int)up16(mono_all);
     L.cold = (int)(up16(mono_all) + up16(part_all));

@@ -71,6 +71,9 @@ struct WarpLayout {
   // FP64 Jacobians (path starts, condition numbers, the FP64 fallback) use A and LU at these
   // offsets of the global slice; −1: one shared A and LU of FP64 size serve both arithmetics
   int cA, cLU;
+  // 1: mixed precision's FP32 Jacobian partial sums go to the FP64 monomial area (dead once the
+  // value rows have been summed) instead of the partial-sum area
+  int jmono;
 };
 // per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
 // counters of profiling builds)

@@ -513,7 +513,9 @@ struct PathTracker {
   __device__ HC_NI void jac_rows(c64 ts64, c64 tt64) {
     HC_PHASE(PH_JACROWS);
     const DevRows& R = P->jac;
-    T* pp = std::is_same<T, c32>::value ? (T*)part : (T*)part_c;
+    // FP32 partial sums: in the FP64 monomial area when the layout says so (val_rows64 has
+    // consumed the FP64 monomials; the FP32 ones this reads lie above them)
+    T* pp = std::is_same<T, c32>::value ? (a->L.jmono ? (T*)mono64 : (T*)part) : (T*)part_c;
     const T* mv;
     const T* cf;
     if constexpr (std::is_same<T, c64>::value) {
