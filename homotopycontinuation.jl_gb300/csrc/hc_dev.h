@@ -82,7 +82,7 @@ constexpr int HC_STATE_BYTES = 1536;
 #else
 constexpr int HC_STATE_BYTES = 1280;
 #endif
-constexpr int HC_NCVEC = 23, HC_NRVEC = 19, HC_NCVEC_COLD = 10, HC_NRVEC_COLD = 16;
+constexpr int HC_NCVEC = 22, HC_NRVEC = 19, HC_NCVEC_COLD = 10, HC_NRVEC_COLD = 16;
 constexpr int HC_LOG_FIELDS = 36;  // doubles per step-log record
 constexpr int HC_NFEAT = 12;       // step features of the learned proposal
 constexpr int HC_NSTATS = 11;      // device counters of a tracking call

@@ -181,7 +181,7 @@ struct PathTracker {
   c32* v32;   // FP32 staging vectors (4 × vn)
   int* ipiv;
   // complex vectors
-  c64 *x, *xh, *xb, *r, *s1, *s2, *tx0, *tx1, *tx2, *tx3, *ptx0, *ptx1, *u;
+  c64 *x, *xh, *xb, *r, *s1, *tx0, *tx1, *tx2, *tx3, *ptx0, *ptx1, *u;
   c64 *sol, *lastp, *pred, *ppred, *smp;
   // real vectors
   double *w, *winv, *rs, *egrs, *egcs, *ais, *ait, *aia, *aic, *vx, *vtx, *dvx, *dvtx, *nu2, *nu1, *lx2, *lx1,
@@ -303,16 +303,15 @@ struct PathTracker {
     xb = cv + 2 * vn;
     r = cv + 3 * vn;
     s1 = cv + 4 * vn;
-    s2 = cv + 5 * vn;
-    tx0 = cv + 6 * vn;
-    tx1 = cv + 7 * vn;
-    tx2 = cv + 8 * vn;
-    tx3 = cv + 9 * vn;
-    ptx0 = cv + 10 * vn;
-    ptx1 = cv + 11 * vn;
-    u = cv + 12 * vn;
-    static_assert(HC_NCVEC - HC_NCVEC_COLD == 13, "sol .. smp are the vectors a cold layout moves");
-    if (!cv_end) cv_end = cv + 13 * vn;
+    tx0 = cv + 5 * vn;
+    tx1 = cv + 6 * vn;
+    tx2 = cv + 7 * vn;
+    tx3 = cv + 8 * vn;
+    ptx0 = cv + 9 * vn;
+    ptx1 = cv + 10 * vn;
+    u = cv + 11 * vn;
+    static_assert(HC_NCVEC - HC_NCVEC_COLD == 12, "sol .. smp are the vectors a cold layout moves");
+    if (!cv_end) cv_end = cv + 12 * vn;
     sol = cv_end + 0 * vn;
     lastp = cv_end + 1 * vn;
     pred = cv_end + 2 * vn;

@@ -68,12 +68,12 @@ def test_automatic_schedule_and_warp_counts():
     T = hc.EndgameTracker(H, hc.TrackerOptions(precision="mixed"))
     T.track_arrays(S[:64])
     assert T.stats()["warps_per_block"] == 16  # as many as fit, at most 16
-    F10, g10 = hc.dense_random_system(10, 3, seed=0)  # 2,880 value terms, 12 warps fit
+    F10, g10 = hc.dense_random_system(10, 3, seed=0)  # 2,880 value terms, 13 warps fit
     H10 = hc.total_degree_homotopy(F10, g10)
     S10 = hc.total_degree_start_solutions(H10.degrees)[:1024]
     T = hc.EndgameTracker(H10, hc.TrackerOptions(precision="mixed"))
     r, x, _, _ = T.track_arrays(S10)
-    assert T.stats()["lockstep"] == 3 and T.stats()["warps_per_block"] == 12
+    assert T.stats()["lockstep"] == 3 and T.stats()["warps_per_block"] == 13
     r0, x0, _, _ = hc.EndgameTracker(H10, hc.TrackerOptions(precision="mixed", lockstep=0)).track_arrays(S10)
     _same(r0, x0, r, x)
     with pytest.raises(hc._lib.HCError):
