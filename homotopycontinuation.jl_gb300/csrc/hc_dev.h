@@ -75,7 +75,7 @@ struct WarpLayout {
   // value rows have been summed) instead of the partial-sum area
   int jmono;
 };
-// per-warp slot of the tracker state object (PathTracker: 1,256 bytes; 1,416 with the phase
+// per-warp slot of the tracker state object (PathTracker: 1,264 bytes; 1,432 with the phase
 // counters of profiling builds)
 #ifdef HC_PHASE_CLOCKS
 constexpr int HC_STATE_BYTES = 1536;
