@@ -1148,6 +1148,9 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
   }
   h->last_warp_bytes = la.L.bytes;
   h->last_table_bytes = la.T.bytes;
+  // a cold layout keeps part of every warp's vectors, A and LU in the global slices: never
+  // launch it without them
+  if (la.L.cold > 0 && !la.cold) return fail(h, HC_ERR_CUDA, "track: cold layout without its global slices");
   CK(cudaMemsetAsync(h->d_counter, 0, (1 + HC_NSTATS + HC_NPHASE) * sizeof(unsigned long long), s));
   if (jit) {
     void* args[] = {(void*)&la};
