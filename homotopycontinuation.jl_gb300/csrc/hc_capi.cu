@@ -1167,22 +1167,33 @@ static int track_device_impl(hc_handle* h, int64_t npaths, const double* d_start
 // Jump check of the host entry points with learned step control. A path that jumps onto
 // another path ends at that path's solution: two nonsingular endpoints coincide. Returns the
 // paths (indices into res/sol) whose nonsingular endpoints coincide with another's within
-// rtol·max(‖x‖∞, 1) — the candidates are swept in order of their first coordinate scaled by
-// ‖x‖∞, which coincident endpoints share up to rounding.
+// rtol·max(‖x‖∞, 1). The candidates are swept in order of a fixed projection p(x) = Σ w·x
+// (weights of absolute sum at most 1, all distinct) scaled by max(‖x‖∞, 1): coincident
+// endpoints' keys differ by at most 2·rtol, and unlike a single coordinate the projection
+// does not put every endpoint whose largest entry is that coordinate on the same key.
 static std::vector<int64_t> coincident_paths(const hc_path_result* res, const double2* sol, int64_t npaths, int n,
                                              double rtol = 1e-8) {
   struct C {
     double key, norm;
     int64_t k;
   };
+  std::vector<double> wt(2 * (size_t)n);
+  for (int i = 0; i < 2 * n; ++i) {  // (0.5 .. 1) / (2n), signs alternating
+    const double f = 0.6180339887498949 * (i + 1);
+    wt[i] = (i & 1 ? -1.0 : 1.0) * (0.5 + 0.5 * (f - std::floor(f))) / (2.0 * n);
+  }
   std::vector<C> c;
+  c.reserve((size_t)npaths);
   for (int64_t k = 0; k < npaths; ++k) {
     if (res[k].return_code != 1 || res[k].singular) continue;  // EndgameTrackerCode success
     const double2* x = sol + k * n;
-    double m = 0;
-    for (int i = 0; i < n; ++i) m = std::max(m, std::max(std::fabs(x[i].x), std::fabs(x[i].y)));
+    double m = 0, p = 0;
+    for (int i = 0; i < n; ++i) {
+      m = std::max(m, std::max(std::fabs(x[i].x), std::fabs(x[i].y)));
+      p += wt[2 * i] * x[i].x + wt[2 * i + 1] * x[i].y;
+    }
     if (!std::isfinite(m)) continue;
-    c.push_back({x[0].x / std::max(m, 1e-300), m, k});
+    c.push_back({p / std::max(m, 1.0), m, k});
   }
   std::sort(c.begin(), c.end(), [](const C& a, const C& b) { return a.key < b.key; });
   std::vector<char> mark(npaths, 0);
